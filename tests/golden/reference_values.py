@@ -1,0 +1,56 @@
+"""Numbers published by the reference (PolyFields.jl), with the file and line they come from.
+
+These are the parity pins of the oracle and of the GPU engine.  Values printed by the
+reference's own runs are copied verbatim; nothing here is computed by this project.
+"""
+import math
+
+# test/test_cell.jl:3-36 — cell volumes
+CELL_VOLUMES = [
+    ((1, "lamellar", 10.0), 10.0),
+    ((2, "square", 10.0), 100.0),
+    ((2, "rectangular", 10.0, 5.0), 50.0),
+    ((2, "hexagonal", 10.0), 86.60254037844385),
+    ((2, "oblique", 10.0, 5.0, math.pi / 4), 35.35533905932737),
+    ((3, "cubic", 10.0), 1000.0),
+    ((3, "tetragonal", 10.0, 5.0), 500.0),
+    ((3, "orthorhombic", 10.0, 5.0, 2.0), 100.0),
+    ((3, "hexagonal", 10.0, 5.0), 433.01270189221924),
+    ((3, "monoclinic", 10.0, 5.0, 2.0, math.pi / 4), 70.71067811865474),
+    ((3, "triclinic", 10.0, 5.0, 2.0, math.pi / 2, math.pi / 2, math.pi / 2), 100.0),
+]
+
+# test/test_species.jl:5-16
+SPECIES = {
+    "point_Nref": 2.0,             # Point(Monomer(vol=2)).Nref
+    "homopolymer_Nref": 100.0,     # Homopolymer(bmon, 100, 1.0, 200).Nref
+    "diblock_f_block_1": 0.4,      # Diblock(amon(vol 2), bmon, 100, 0.25, ...).f_block[1]
+    "diblock_Nref_block_2": 75.0,  # ... .Nref_block[2]
+    "multiblock_fraction_1": 2 / 3,
+}
+
+# README.md:62-79 — scft! on 64x1x1 lamellar, Diblock N100 f0.5 Ns100, chi 0.2, Anderson
+# nhist 10, DomainUpdater nskip 5 / nper 20, ftol = stol = 1e-4.  Converged state:
+README_LAMELLAR = {
+    "L": 16.528709413909947,
+    "fhelm": 0.0812381288285528,
+    "ferr": 5.0874415525661515e-6,
+    "serr": 1.6582423877606872e-6,
+    "nsteps": 36,
+}
+
+# examples/examples.ipynb cell 12 output: ABC blend (Point C vol 1 phi 0.4, homopolymers
+# A, B vol 2 N100 phi 0.3 each; chi_AB 0.5, chi_AC = chi_BC = 1.25) on 256x1x1, L = 20.
+# The saved seed examples/seeds/abc_blend_1d.json is that converged state, so residuals!
+# + field_error + free_energy on the seed reproduce these to rounding.
+BLEND_FINAL = {"ferr": 9.9617272806509e-6, "fhelm": -0.04720567097567993}
+
+# examples/examples.ipynb cell 8 output: 128x128 hexagonal cylinders, Diblock N100 f0.3
+# Ns100, chi 0.3, cell a = 18.381681210100236 (seed examples/seeds/cyl2d.json is 64x64).
+CYL2D_FINAL_128 = {"ferr": 9.910317272221094e-6, "fhelm": 0.10659231121049459,
+                   "a": 18.381681210100236}
+
+# examples/examples.ipynb cell 4 output: 128x1x1 lamellar, Diblock N100 f0.5 Ns100, chi
+# 0.25, L = 13.100000015310233 (seed examples/seeds/lam1d.json is 64x1x1); converged at
+# step 0.
+LAM1D_FINAL_128 = {"ferr": 9.713161299981836e-6, "fhelm": 0.10211268214323928}
