@@ -1,0 +1,164 @@
+/*
+ * polyfields_gpu.h — C ABI of libpolyfields_gpu.so, the GB300 SCFT engine that stands in for
+ * PolyFields.jl's `scft!(sys, AndersonUpdater; domain = DomainUpdater, opts = SCFTOptions)`.
+ *
+ * The reference is pure Julia with no C interface; each entry point below replaces the Julia
+ * function cited beside it (file:line within the PolyFields.jl project).  A Julia binding
+ * calls these through `ccall`; the Python package in
+ * polyfields.jl_gb300/polyfields calls them through ctypes.
+ *
+ * Conventions
+ *  - Every function returns an int status (PF_OK = 0).  On failure the handle's
+ *    pf_last_error() string says why; the Julia shim raises it as the reference's error().
+ *  - Grids are float64 arrays of Nx*Ny*Nz values, x fastest (the memory order of the
+ *    reference's Array{Float64,3}[x, y, z]); dims must be in descending order, as the
+ *    reference's FieldSystem requires (src/system/system.jl:55-58).
+ *  - Host arrays are only read or written during the call; device memory is owned by the
+ *    handle.  One handle is used by one host thread at a time; it owns one CUDA stream.
+ *  - Monomers are addressed by their integer id, species by their 0-based order of addition.
+ */
+#ifndef POLYFIELDS_GPU_H
+#define POLYFIELDS_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum pf_status {
+  PF_OK = 0,
+  PF_EARG = 1,        /* invalid argument (reference: ArgumentError / AssertionError / error) */
+  PF_ECUDA = 2,       /* CUDA runtime failure */
+  PF_ENAN = 3,        /* "Diverging field updater -- breaking." (src/simulate.jl:109-111) */
+  PF_ESINGULAR = 4,   /* "Error inverting Umn matrix" (src/updaters/anderson.jl:184-189) */
+  PF_ETIMEOUT = 5,    /* a bounded device wait gave up */
+  PF_ESTATE = 6,      /* call out of order (e.g. step before setup) */
+  PF_ENOMEM = 7,      /* device allocation failed */
+  PF_EUNSUPPORTED = 8 /* grid length outside the supported FFT sizes */
+};
+
+enum pf_precision {
+  PF_FP64 = 0,  /* propagators and FFTs in float64 (the reference's arithmetic) */
+  PF_FP32 = 1   /* propagators and FFTs in float32; densities, residuals, Gram, stress sums stay float64 */
+};
+
+enum pf_grid_kind { PF_FIELD = 0, PF_DENSITY = 1, PF_RESIDUAL = 2, PF_POTENTIAL = 3 };
+
+typedef struct pf_system pf_system;
+
+/* SCFTOptions (src/simulate.jl:12-19) plus the mixed-precision switch.  When
+ * mixed_switch_ferr > 0 and the handle runs PF_FP32, scft switches to PF_FP64 once
+ * ferr < mixed_switch_ferr and continues to ftol/stol (FP64 polish). */
+typedef struct pf_scft_options {
+  int nsteps;
+  int nsout;
+  int nsave;
+  int pad0;
+  double ftol;
+  double stol;
+  double mixed_switch_ferr;
+} pf_scft_options;
+
+/* SCFTResults (src/simulate.jl:26-33) plus the step at which the precision switched (-1 if never). */
+typedef struct pf_scft_results {
+  double time;
+  int nsteps;
+  int converged;
+  double ferr;
+  double serr;
+  double fhelm;
+  int switch_step;
+  int pad0;
+} pf_scft_results;
+
+/* ---- library ---- */
+int pf_version(void);                       /* 100 * major + minor */
+const char* pf_status_string(int status);
+
+/* ---- FieldSystem (src/system/system.jl:51-76) ---- */
+int pf_system_create(pf_system** out, int nx, int ny, int nz, int precision);
+int pf_system_destroy(pf_system* sys);
+const char* pf_last_error(const pf_system* sys);
+int pf_set_precision(pf_system* sys, int precision);
+int pf_get_precision(const pf_system* sys, int* precision);
+
+/* UnitCell(dim, crystal, params) + add_cell!  (src/system/cell.jl:31-52, system.jl:102-106).
+ * crystal is the reference's Symbol name without ':' ("lamellar", "hexagonal", "cubic", ...). */
+int pf_set_cell(pf_system* sys, int dim, const char* crystal, const double* params, int nparams);
+/* cell.params, cell.volume (src/system/cell.jl:14-29) */
+int pf_get_cell(const pf_system* sys, double* params, int nparams, double* volume);
+/* R and G basis matrices, row-major 3x3 (src/system/cell.jl:113-118) */
+int pf_get_basis(const pf_system* sys, double* R, double* G);
+
+/* add_monomer! (src/system/system.jl:113-128) */
+int pf_add_monomer(pf_system* sys, int id, double vol, double charge);
+/* Multiblock(mon_block, N_block, b_block, Ns) + add_species!(sys, chain, phi)
+ * (src/species/multiblock.jl:32-60, src/system/system.jl:137-161). */
+int pf_add_multiblock(pf_system* sys, int nblocks, const int* block_mids, const int* N_block,
+                      const double* b_block, int Ns, double phi);
+/* Point(mon) + add_species! (src/species/point.jl:9-22) */
+int pf_add_point(pf_system* sys, int mid, double phi);
+/* FloryInteraction set_interaction! + add_interaction! (src/interactions/flory.jl:36-49) */
+int pf_set_flory(pf_system* sys, int mid_a, int mid_b, double chi);
+
+/* chain_grid(N_block .* vol, Ns) of a species: Ns after adjustment, Nref, begin_block (nblocks+1,
+ * 1-based as in the reference) and ds_block (src/species/base.jl:27-56). */
+int pf_species_info(const pf_system* sys, int isp, int* Ns, double* Nref, int* begin_block, double* ds_block,
+                    int max_blocks);
+
+/* ---- grids ---- */
+/* fieldinit!(sys, fields::Dict) for one monomer without the final residuals! (src/fileio.jl:25-54). */
+int pf_set_field(pf_system* sys, int mid, const double* w);
+/* sys.fields / density / residuals / potentials[mid] -> host (Ng doubles) */
+int pf_get_grid(pf_system* sys, int kind, int mid, double* out);
+/* chain.q[s] or chain.qc[s] (0-based s) of a multiblock species -> host */
+int pf_get_propagator(pf_system* sys, int isp, int conjugate, int s, double* out);
+
+/* ---- hot path ---- */
+int pf_validate(pf_system* sys);                          /* validate(sys)     system.jl:192-237 */
+int pf_density(pf_system* sys);                           /* density!(sys)     system.jl:266-289 */
+int pf_residuals(pf_system* sys);                         /* residuals!(sys)   system.jl:317-340 */
+int pf_free_energy(pf_system* sys, double* out);          /* free_energy(sys)  system.jl:402-433 */
+int pf_free_energy_bulk(pf_system* sys, double* out);     /* free_energy_bulk  system.jl:440-458 */
+int pf_field_error(pf_system* sys, double* out);          /* field_error(sys)  system.jl:470-486 */
+int pf_scfstress(pf_system* sys, double* out, int nparams); /* scfstress(sys)  system.jl:384-395 */
+int pf_species_q(pf_system* sys, int isp, double* Q);     /* species.Q after density! */
+
+/* AndersonUpdater(; nhist = 50, iter_euler = 1, lam_euler = 0.01) (src/updaters/anderson.jl:36-47).
+ * Replaces the handle's Anderson updater with a fresh one that is not yet set up. */
+int pf_anderson_create(pf_system* sys, int nhist, int iter_euler, double lam_euler);
+/* setup!(::AndersonUpdater, sys) (src/updaters/anderson.jl:54-92): allocates the history and
+ * stores the current fields; keeps the history when already set up. */
+int pf_anderson_setup(pf_system* sys);
+/* step!(::AndersonUpdater) (src/updaters/anderson.jl:98-228) */
+int pf_anderson_step(pf_system* sys);
+/* DomainUpdater(; nper = 10, nskip = 200, lam = 0.1, pmax = 1.0, rlxn = 0.5) (src/updaters/domain.jl:20-24) */
+int pf_domain_create(pf_system* sys, int nper, int nskip, double lam, double pmax, double rlxn);
+/* setup!(::DomainUpdater, sys) (src/updaters/domain.jl:32-42): computes the stress. */
+int pf_domain_setup(pf_system* sys);
+/* step!(::DomainUpdater; nsteps) (src/updaters/domain.jl:50-92) */
+int pf_domain_step(pf_system* sys, int nsteps);
+/* stress_error(domain) (src/updaters/domain.jl:30) */
+int pf_domain_stress_error(pf_system* sys, double* out);
+
+/* scft!(sys, AndersonUpdater; domain, opts) (src/simulate.jl:60-148) with the updaters created
+ * by pf_anderson_create (required) and pf_domain_create (used when use_domain != 0). */
+int pf_scft(pf_system* sys, const pf_scft_options* opts, int use_domain, pf_scft_results* out);
+
+/* ---- low level: PseudoSpectralSolver update! + propagate! (src/system/mde.jl:43-81) ----
+ * Propagates nsteps RK2 steps from qin with the operators of (omega, vol, b, ds) on the
+ * handle's current cell; qout receives the last step.  Host arrays. */
+int pf_propagate(pf_system* sys, const double* omega, double vol, double b, double ds,
+                 const double* qin, double* qout, int nsteps);
+
+/* ---- measurement ---- */
+/* Device time (ms) of the last density solve's propagator launches, measured with CUDA
+ * events on the handle's stream; 0 if not recorded.  Enable with pf_set_timing(sys, 1). */
+int pf_set_timing(pf_system* sys, int enable);
+int pf_last_timing(const pf_system* sys, double* propagate_ms, double* density_ms, int* mde_steps);
+/* Synchronise the handle's stream. */
+int pf_synchronize(pf_system* sys);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* POLYFIELDS_GPU_H */

@@ -1,0 +1,1467 @@
+// Host engine and C ABI of libpolyfields_gpu.so.
+//
+// A pf_system is the GPU counterpart of the reference's FieldSystem
+// (src/system/system.jl:22-49): grid, unit cell, monomers, species, Flory interactions and
+// the device state (fields, potentials, residuals, densities, propagators, operators),
+// plus the Anderson and Domain updaters (src/updaters/anderson.jl, domain.jl) and the
+// scft! driver loop (src/simulate.jl:60-148).  The orchestration runs on the host; every
+// grid-sized operation runs on the device, on the handle's own stream.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include <array>
+#include <chrono>
+
+#include "pf_kernels.h"
+#include "polyfields_gpu.h"
+
+namespace pf {
+
+// ------------------------------------------------------------------ errors
+struct PFError : std::runtime_error {
+  int code;
+  PFError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define PF_CU(call)                                                                                  \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess)                                                                           \
+      throw pf::PFError(e_ == cudaErrorMemoryAllocation ? pf::E_NOMEM : pf::E_CUDA,                  \
+                        std::string("CUDA error ") + cudaGetErrorString(e_) + " at " #call);         \
+  } while (0)
+
+static void check_launch() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw PFError(E_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+}
+
+// Owning device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  void alloc(size_t n) {
+    if (n == bytes && p) return;
+    release();
+    if (n == 0) return;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw PFError(E_NOMEM, std::string("cudaMalloc of ") + std::to_string(n) + " bytes failed: " + cudaGetErrorString(e));
+    }
+    bytes = n;
+  }
+  template <typename T>
+  T* as() const { return static_cast<T*>(p); }
+};
+
+// ------------------------------------------------------------------ cell geometry (host)
+// src/system/basis.jl and src/system/cell.jl.  Matrices are row-major 3x3, the Bravais
+// vectors a_c are the columns of R and the reciprocal vectors b_c the columns of G.
+using Mat3 = std::array<double, 9>;
+
+static bool isapprox(double a, double b) {
+  const double rtol = std::sqrt(2.220446049250313e-16);
+  return std::fabs(a - b) <= rtol * std::max(std::fabs(a), std::fabs(b));
+}
+
+static Mat3 basis_matrix(double a, double b, double c, double alpha, double beta, double gamma) {
+  const double p2 = M_PI / 2;
+  Mat3 R{};
+  if (isapprox(alpha, p2) && isapprox(beta, p2) && isapprox(gamma, p2)) {
+    R = {a, 0, 0, 0, b, 0, 0, 0, c};
+    return R;
+  }
+  const double ca = isapprox(alpha, p2) ? 0.0 : std::cos(alpha);
+  const double cb = isapprox(beta, p2) ? 0.0 : std::cos(beta);
+  double cg, sg;
+  if (isapprox(gamma, p2)) {
+    cg = 0.0;
+    sg = 1.0;
+  } else {
+    cg = std::cos(gamma);
+    sg = std::sin(gamma);
+  }
+  const double ax = a, bx = b * cg, by = b * sg, cx = c * cb, cy = c * (ca - cb * cg) / sg;
+  const double cz = std::sqrt(c * c - cx * cx - cy * cy);
+  R = {ax, bx, cx, 0.0, by, cy, 0.0, 0.0, cz};
+  return R;
+}
+
+static int crystal_nparams(int dim, const std::string& c) {
+  if (dim == 1 && c == "lamellar") return 1;
+  if (dim == 2) {
+    if (c == "square" || c == "hexagonal") return 1;
+    if (c == "rectangular") return 2;
+    if (c == "oblique") return 3;
+  }
+  if (dim == 3) {
+    if (c == "cubic" || c == "pnna" || c == "fddd1") return 1;
+    if (c == "tetragonal" || c == "hexagonal") return 2;
+    if (c == "orthorhombic") return 3;
+    if (c == "monoclinic") return 4;
+    if (c == "triclinic") return 6;
+  }
+  return -1;
+}
+
+static Mat3 make_basis(int dim, const std::string& c, const std::vector<double>& p) {
+  const double pi = M_PI;
+  if (dim == 1) return basis_matrix(p[0], 1.0, 1.0, pi / 2, pi / 2, pi / 2);
+  if (dim == 2) {
+    if (c == "square") return basis_matrix(p[0], p[0], 1.0, pi / 2, pi / 2, pi / 2);
+    if (c == "rectangular") return basis_matrix(p[0], p[1], 1.0, pi / 2, pi / 2, pi / 2);
+    if (c == "hexagonal") return basis_matrix(p[0], p[0], 1.0, pi / 2, pi / 2, pi / 3);
+    return basis_matrix(p[0], p[1], 1.0, pi / 2, pi / 2, p[2]);  // oblique
+  }
+  if (c == "cubic") return basis_matrix(p[0], p[0], p[0], pi / 2, pi / 2, pi / 2);
+  if (c == "tetragonal") return basis_matrix(p[0], p[0], p[1], pi / 2, pi / 2, pi / 2);
+  if (c == "orthorhombic") return basis_matrix(p[0], p[1], p[2], pi / 2, pi / 2, pi / 2);
+  if (c == "hexagonal") return basis_matrix(p[0], p[0], p[1], pi / 2, pi / 2, pi / 3);
+  if (c == "monoclinic") return basis_matrix(p[0], p[1], p[2], pi / 2, p[3], pi / 2);
+  if (c == "triclinic") return basis_matrix(p[0], p[1], p[2], p[3], p[4], p[5]);
+  if (c == "pnna") return basis_matrix(2.0 * p[0], std::sqrt(3.0) * p[0], p[0], pi / 2, pi / 2, pi / 2);
+  return basis_matrix(p[0], std::sqrt(3.0) * p[0], 2.0 * std::sqrt(3.0) * p[0], pi / 2, pi / 2, pi / 2);  // fddd1
+}
+
+static double det3(const Mat3& m) {
+  return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) + m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+static Mat3 inv3(const Mat3& m) {
+  const double d = det3(m);
+  Mat3 r;
+  r[0] = (m[4] * m[8] - m[5] * m[7]) / d;
+  r[1] = (m[2] * m[7] - m[1] * m[8]) / d;
+  r[2] = (m[1] * m[5] - m[2] * m[4]) / d;
+  r[3] = (m[5] * m[6] - m[3] * m[8]) / d;
+  r[4] = (m[0] * m[8] - m[2] * m[6]) / d;
+  r[5] = (m[2] * m[3] - m[0] * m[5]) / d;
+  r[6] = (m[3] * m[7] - m[4] * m[6]) / d;
+  r[7] = (m[1] * m[6] - m[0] * m[7]) / d;
+  r[8] = (m[0] * m[4] - m[1] * m[3]) / d;
+  return r;
+}
+
+struct Cell {
+  int dim = 0;
+  std::string crystal;
+  std::vector<double> params;
+  double volume = 0.0;
+  Mat3 R{}, G{};
+  // dR[(i*3+j)*kMaxParams+k] etc.
+  std::vector<double> dR, dG, dRR, dGG;
+  int np() const { return (int)params.size(); }
+
+  // update!(cell) (cell.jl:96-109) without the grids (they are device-side).
+  void update() {
+    R = make_basis(dim, crystal, params);
+    Mat3 Ri = inv3(R);
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) G[r * 3 + c] = 2 * M_PI * Ri[c * 3 + r];
+    volume = det3(R);
+    dbasis();
+    ddbasis();
+  }
+  double& at(std::vector<double>& a, int i, int j, int k) { return a[(i * 3 + j) * kMaxParams + k]; }
+  void dbasis() {  // cell.jl:120-231
+    dR.assign(9 * kMaxParams, 0.0);
+    dG.assign(9 * kMaxParams, 0.0);
+    const auto& p = params;
+    const std::string& c = crystal;
+    if (dim == 1) {
+      if (c == "lamellar") at(dR, 0, 0, 0) = 1.0;
+    } else if (dim == 2) {
+      if (c == "square") {
+        at(dR, 0, 0, 0) = 1.0;
+        at(dR, 1, 1, 0) = 1.0;
+      } else if (c == "rectangular") {
+        at(dR, 0, 0, 0) = 1.0;
+        at(dR, 1, 1, 1) = 1.0;
+      } else if (c == "hexagonal") {
+        at(dR, 0, 0, 0) = 1.0;
+        at(dR, 0, 1, 0) = 0.5;
+        at(dR, 1, 1, 0) = std::sqrt(0.75);
+      } else if (c == "oblique") {
+        const double b = p[1], gamma = p[2];
+        at(dR, 0, 0, 0) = 1.0;
+        at(dR, 0, 1, 1) = std::cos(gamma);
+        at(dR, 1, 1, 1) = std::sin(gamma);
+        at(dR, 0, 1, 2) = -b * std::sin(gamma);
+        at(dR, 1, 1, 2) = b * std::cos(gamma);
+      }
+    } else if (dim == 3) {
+      if (c == "cubic") {
+        at(dR, 0, 0, 0) = at(dR, 1, 1, 0) = at(dR, 2, 2, 0) = 1.0;
+      } else if (c == "tetragonal") {
+        at(dR, 0, 0, 0) = at(dR, 1, 1, 0) = 1.0;
+        at(dR, 2, 2, 1) = 1.0;
+      } else if (c == "orthorhombic") {
+        at(dR, 0, 0, 0) = at(dR, 1, 1, 1) = at(dR, 2, 2, 2) = 1.0;
+      } else if (c == "hexagonal") {
+        at(dR, 0, 0, 0) = 1.0;
+        at(dR, 0, 1, 0) = 0.5;
+        at(dR, 1, 1, 0) = std::sqrt(0.75);
+        at(dR, 2, 2, 1) = 1.0;
+      } else if (c == "monoclinic") {
+        const double cc = p[2], beta = p[3];
+        at(dR, 0, 0, 0) = 1.0;
+        at(dR, 1, 1, 1) = 1.0;
+        at(dR, 0, 2, 2) = std::cos(beta);
+        at(dR, 2, 2, 2) = std::sin(beta);
+        at(dR, 0, 2, 3) = -cc * std::sin(beta);
+        at(dR, 2, 2, 3) = cc * std::cos(beta);
+      } else if (c == "triclinic") {
+        const double b = p[1], cc = p[2], alpha = p[3], beta = p[4], gamma = p[5];
+        const double cy = R[1 * 3 + 2], cz = R[2 * 3 + 2];
+        const double sa = std::sin(alpha), ca = std::cos(alpha), sb = std::sin(beta), cb = std::cos(beta);
+        const double sg = std::sin(gamma), cg = std::cos(gamma), tg = std::tan(gamma);
+        at(dR, 0, 0, 0) = 1.0;
+        at(dR, 0, 1, 1) = cg;
+        at(dR, 1, 1, 1) = sg;
+        at(dR, 0, 2, 2) = cb;
+        at(dR, 1, 2, 2) = cy / cc;
+        at(dR, 2, 2, 2) = cz / cc;
+        at(dR, 1, 2, 3) = -cc * sa / sg;
+        at(dR, 2, 2, 3) = cc * cc * (ca - cb * cg) * sa / (sg * sg) / cz;
+        at(dR, 0, 2, 4) = -cc * sb;
+        at(dR, 1, 2, 4) = cc * sb / tg;
+        at(dR, 2, 2, 4) = cc * cc * (-ca / tg + cb / sg) * sb / sg / cz;
+        at(dR, 0, 1, 5) = -b * sg;
+        at(dR, 1, 1, 5) = b * cg;
+        at(dR, 1, 2, 5) = cc * (-ca / tg + cb / sg) / sg;
+        at(dR, 2, 2, 5) = cc * cc * ((2 + std::cos(2 * alpha) + std::cos(2 * beta)) / tg -
+                                     ca * cb * (3 + std::cos(2 * gamma)) / sg) / (sg * sg) / cz / 2;
+      } else if (c == "pnna") {
+        at(dR, 0, 0, 0) = 2.0;
+        at(dR, 1, 1, 0) = std::sqrt(3.0);
+        at(dR, 2, 2, 0) = 1.0;
+      } else if (c == "fddd1") {
+        at(dR, 0, 0, 0) = 1.0;
+        at(dR, 1, 1, 0) = std::sqrt(3.0);
+        at(dR, 2, 2, 0) = 2.0 * std::sqrt(3.0);
+      }
+    }
+    for (int k = 0; k < np(); ++k)
+      for (int i = 0; i < dim; ++i)
+        for (int j = 0; j < dim; ++j)
+          for (int l = 0; l < dim; ++l)
+            for (int m = 0; m < dim; ++m) at(dG, i, j, k) -= G[i * 3 + l] * at(dR, m, l, k) * G[m * 3 + j];
+    for (auto& v : dG) v /= 2 * M_PI;
+  }
+  void ddbasis() {  // cell.jl:233-258 (R transposed as in the reference)
+    dRR.assign(9 * kMaxParams, 0.0);
+    dGG.assign(9 * kMaxParams, 0.0);
+    for (int k = 0; k < np(); ++k)
+      for (int i = 0; i < dim; ++i)
+        for (int j = 0; j < dim; ++j)
+          for (int l = 0; l < dim; ++l) {
+            at(dRR, i, j, k) += R[l * 3 + i] * at(dR, l, j, k) + R[l * 3 + j] * at(dR, l, i, k);
+            at(dGG, i, j, k) += G[l * 3 + i] * at(dG, l, j, k) + G[l * 3 + j] * at(dG, l, i, k);
+          }
+  }
+};
+
+// Host LU with partial pivoting + explicit inverse (the reference's inv()).
+static bool lu_inverse(std::vector<double> a, int n, std::vector<double>& inv) {
+  std::vector<int> perm(n);
+  for (int i = 0; i < n; ++i) perm[i] = i;
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    double best = std::fabs(a[k * n + k]);
+    for (int i = k + 1; i < n; ++i)
+      if (std::fabs(a[i * n + k]) > best) {
+        best = std::fabs(a[i * n + k]);
+        p = i;
+      }
+    if (a[p * n + k] == 0.0) return false;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) std::swap(a[k * n + j], a[p * n + j]);
+      std::swap(perm[k], perm[p]);
+    }
+    for (int i = k + 1; i < n; ++i) a[i * n + k] /= a[k * n + k];
+    for (int i = k + 1; i < n; ++i)
+      for (int j = k + 1; j < n; ++j) a[i * n + j] -= a[i * n + k] * a[k * n + j];
+  }
+  inv.assign(n * n, 0.0);
+  std::vector<double> y(n);
+  for (int col = 0; col < n; ++col) {
+    for (int i = 0; i < n; ++i) {
+      double s = (perm[i] == col) ? 1.0 : 0.0;
+      for (int j = 0; j < i; ++j) s -= a[i * n + j] * y[j];
+      y[i] = s;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double s = y[i];
+      for (int j = i + 1; j < n; ++j) s -= a[i * n + j] * inv[j * n + col];
+      inv[i * n + col] = s / a[i * n + i];
+    }
+  }
+  return true;
+}
+
+// ------------------------------------------------------------------ species
+struct Species {
+  int kind = 0;  // 0 multiblock, 1 point
+  double phi = 0.0, mu = 0.0, Q = 0.0, Nref = 0.0;
+  std::vector<int> mids;  // sorted monomer ids
+  // multiblock (src/species/multiblock.jl:5-60)
+  int Ns = 0, N = 0;
+  std::vector<int> mid_block, N_block, begin_block;  // begin_block 1-based
+  std::vector<double> b_block, ds_block, Nref_block, f_block;
+  // device, per precision (0 = FP64, 1 = FP32)
+  DevBuf q[2], qc[2];
+  std::vector<std::unique_ptr<DevBuf>> lw[2], ld[2];
+  DevBuf ops[2];  // StepOp<T> of the forward then backward job
+  DevBuf kbuf[2][2];
+  int ld_version[2] = {-1, -1};
+  DevBuf Qdev;
+  bool Q_valid = false;
+  int nblocks() const { return (int)N_block.size(); }
+  double monomer_fraction(int mid) const {
+    if (kind == 1) return (mids[0] == mid) ? 1.0 : 0.0;
+    double f = 0.0;
+    for (int b = 0; b < nblocks(); ++b)
+      if (mid_block[b] == mid) f += f_block[b];
+    return f;
+  }
+};
+
+// chain_grid (src/species/base.jl:27-56)
+static void chain_grid(const std::vector<double>& Nb, int Ns, double& N, std::vector<int>& begin_block,
+                       std::vector<double>& ds_block) {
+  N = 0.0;
+  for (double v : Nb) N += v;
+  const int nb = (int)Nb.size();
+  const double ds = N / Ns;
+  begin_block.assign(nb + 1, 0);
+  ds_block.assign(nb, 0.0);
+  int bgn = 1;
+  begin_block[0] = bgn;
+  for (int i = 0; i < nb; ++i) {
+    int Ns_half = (int)std::floor(Nb[i] / ds / 2.0 + 0.5);
+    if (Ns_half == 0) {
+      Ns_half = 1;
+      ds_block[i] = Nb[i] / 2.0;
+    } else {
+      ds_block[i] = Nb[i] / Ns_half / 2.0;
+    }
+    bgn = bgn + Ns_half * 2;
+    begin_block[i + 1] = bgn;
+  }
+}
+
+// ------------------------------------------------------------------ the system
+struct System {
+  int nx, ny, nz;
+  long ng, nk;
+  int prec;         // current precision of the propagators
+  int last_prec = -1;  // precision of the last density solve
+  cudaStream_t st = nullptr;
+  std::string err;
+
+  Cell cell;
+  bool has_cell = false;
+  int cell_version = 0;
+  int dksq_version = -1;
+
+  std::map<int, std::pair<double, double>> monomers;  // id -> (vol, charge)
+  std::vector<int> mon_ids;                            // sorted ids; index = position
+  std::map<std::pair<int, int>, double> chis;          // ordered pair -> chi
+  std::vector<std::unique_ptr<Species>> species;
+
+  DevBuf w, pot, res, rho;   // nmon * ng doubles
+  DevBuf part, sums, stats4, packed, cn, status;
+  DevBuf twid[2];
+  DevBuf dksq;
+  DevBuf jobs[2];
+  int njobs = 0, maxsteps = 0;
+  bool jobs_dirty[2] = {true, true};
+  bool timing = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double t_prop_ms = 0.0, t_dens_ms = 0.0;
+  int mde_steps = 0;
+
+  // Anderson updater (src/updaters/anderson.jl:13-47)
+  struct Anderson {
+    bool exists = false, is_setup = false;
+    int nhist = 50, iter = 0, iter_hist = 0, iter_euler = 1, base = 0;
+    double lam = 0.0, lam_euler = 0.01;
+    DevBuf res_hist, field_hist;
+    void reset() {
+      exists = is_setup = false;
+      nhist = 50;
+      iter = iter_hist = 0;
+      iter_euler = 1;
+      base = 0;
+      lam = 0.0;
+      lam_euler = 0.01;
+      res_hist.release();
+      field_hist.release();
+    }
+  } and_;
+  // Domain updater (src/updaters/domain.jl:7-24)
+  struct Domain {
+    bool exists = false, is_setup = false;
+    int nper = 10, nskip = 200;
+    double lam = 0.1, pmax = 1.0, rlxn = 0.5;
+    std::vector<double> oldparams, step, stress, dstress;
+  } dom;
+
+  System(int x, int y, int z, int p) : nx(x), ny(y), nz(z), prec(p) {
+    ng = (long)nx * ny * nz;
+    nk = (long)(nx / 2 + 1) * ny * nz;
+    PF_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    part.alloc(sizeof(double) * (size_t)kRedBlocks * 4 * (kMaxMon + 1) + sizeof(double) * 2048 * 2 * 152);
+    sums.alloc(sizeof(double) * 4 * kMaxMon);
+    stats4.alloc(sizeof(double) * 8);
+    packed.alloc(sizeof(double) * 4096);
+    cn.alloc(sizeof(double) * kMaxHist);
+    status.alloc(sizeof(int) * 4);
+    build_twiddles<double>(0);
+    build_twiddles<float>(1);
+    for (auto& e : ev) PF_CU(cudaEventCreate(&e));
+  }
+  ~System() {
+    if (st) cudaStreamSynchronize(st);
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  int nmon() const { return (int)mon_ids.size(); }
+  int mon_index(int id) const {
+    auto it = std::find(mon_ids.begin(), mon_ids.end(), id);
+    if (it == mon_ids.end()) throw PFError(E_ARG, "monomer with id = " + std::to_string(id) + " not present in system");
+    return (int)(it - mon_ids.begin());
+  }
+  // pencils per tile of the z pass
+  static int zM(int p) { return p == 1 ? z_tile_pencils<float>() : z_tile_pencils<double>(); }
+
+  template <typename T>
+  void build_twiddles(int p) {
+    const int lens[3] = {nx, ny, nz};
+    std::vector<Cx<T>> h;
+    for (int a = 0; a < 3; ++a) {
+      const int n = lens[a];
+      for (int m = 0; m < n; ++m) {
+        // exp(-2 pi i m / n) with the angle reduced to the first octant for accuracy
+        const long double ang = -2.0L * 3.141592653589793238462643383279502884L * (long double)m / (long double)n;
+        h.push_back(cx<T>((T)std::cos(ang), (T)std::sin(ang)));
+      }
+    }
+    twid[p].alloc(sizeof(Cx<T>) * h.size());
+    PF_CU(cudaMemcpy(twid[p].p, h.data(), sizeof(Cx<T>) * h.size(), cudaMemcpyHostToDevice));
+  }
+  template <typename T>
+  Twiddles<T> tw(int p) const {
+    const Cx<T>* b = twid[p].as<Cx<T>>();
+    return Twiddles<T>{b, b + nx, b + nx + ny};
+  }
+
+  CellGeom geom() const {
+    CellGeom g{};
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    g.dim = cell.dim;
+    for (int i = 0; i < 9; ++i) g.G[i] = cell.G[i];
+    for (int i = 0; i < 9 * kMaxParams; ++i) g.dGG[i] = cell.dGG[i];
+    return g;
+  }
+
+  MonomerSet monomer_set() const {
+    MonomerSet ms{};
+    ms.nmon = nmon();
+    for (int a = 0; a < nmon(); ++a) ms.vol[a] = monomers.at(mon_ids[a]).first;
+    for (auto& kv : chis) {
+      const int a = mon_index(kv.first.first), b = mon_index(kv.first.second);
+      ms.chi[a * kMaxMon + b] = kv.second;
+      ms.chi[b * kMaxMon + a] = kv.second;
+    }
+    return ms;
+  }
+
+  double* grid_ptr(DevBuf& b, int mid) { return b.as<double>() + (long)mon_index(mid) * ng; }
+
+  // ---------------------------------------------------------------- composition
+  void add_monomer(int id, double vol, double charge) {
+    if (nmon() >= kMaxMon && !monomers.count(id)) throw PFError(E_ARG, "too many monomer types (max 8)");
+    std::vector<int> old_ids = mon_ids;
+    monomers[id] = {vol, charge};
+    mon_ids.clear();
+    for (auto& kv : monomers) mon_ids.push_back(kv.first);
+    // re-layout the per-monomer grids (add_monomer! zero-initialises the new monomer)
+    DevBuf* bufs[4] = {&w, &pot, &res, &rho};
+    for (DevBuf* b : bufs) {
+      DevBuf nb;
+      nb.alloc(sizeof(double) * ng * nmon());
+      PF_CU(cudaMemsetAsync(nb.p, 0, nb.bytes, st));
+      if (b->p) {
+        for (size_t i = 0; i < old_ids.size(); ++i) {
+          if (old_ids[i] == id) continue;
+          const int ni = mon_index(old_ids[i]);
+          PF_CU(cudaMemcpyAsync(nb.as<double>() + ni * ng, b->as<double>() + i * ng, sizeof(double) * ng,
+                                cudaMemcpyDeviceToDevice, st));
+        }
+      }
+      PF_CU(cudaStreamSynchronize(st));
+      std::swap(b->p, nb.p);
+      std::swap(b->bytes, nb.bytes);
+    }
+    and_.reset();
+    jobs_dirty[0] = jobs_dirty[1] = true;
+  }
+
+  void add_multiblock(int nb, const int* bm, const int* Nb, const double* bb, int Ns, double phi) {
+    if (nb < 1 || nb > 2 * kMaxMon) throw PFError(E_ARG, "number of blocks must be in [1, 16]");
+    if (Ns < 1) throw PFError(E_ARG, "Ns must be positive");
+    auto sp = std::make_unique<Species>();
+    sp->kind = 0;
+    std::set<int> ids;
+    for (int i = 0; i < nb; ++i) {
+      if (!monomers.count(bm[i]))
+        throw PFError(E_ARG, "Species contains monomer with id = " + std::to_string(bm[i]) + " not present in system.");
+      ids.insert(bm[i]);
+      sp->mid_block.push_back(bm[i]);
+      sp->N_block.push_back(Nb[i]);
+      sp->b_block.push_back(bb[i]);
+      sp->N += Nb[i];
+      sp->Nref_block.push_back(monomers[bm[i]].first * Nb[i]);
+    }
+    sp->mids.assign(ids.begin(), ids.end());
+    chain_grid(sp->Nref_block, Ns, sp->Nref, sp->begin_block, sp->ds_block);
+    for (double v : sp->Nref_block) sp->f_block.push_back(v / sp->Nref);
+    sp->Ns = sp->begin_block.back() - 1;  // multiblock.jl:56-59
+    if (phi <= 0.0) throw PFError(E_ARG, "Bulk volume fraction must be 0 < phi <= 1.");
+    sp->phi = phi;
+    sp->Qdev.alloc(sizeof(double));
+    species.push_back(std::move(sp));
+    jobs_dirty[0] = jobs_dirty[1] = true;
+  }
+
+  void add_point(int mid, double phi) {
+    if (!monomers.count(mid))
+      throw PFError(E_ARG, "Species contains monomer with id = " + std::to_string(mid) + " not present in system.");
+    if (phi <= 0.0) throw PFError(E_ARG, "Bulk volume fraction must be 0 < phi <= 1.");
+    auto sp = std::make_unique<Species>();
+    sp->kind = 1;
+    sp->mids = {mid};
+    sp->Nref = monomers[mid].first;
+    sp->phi = phi;
+    sp->Qdev.alloc(sizeof(double));
+    species.push_back(std::move(sp));
+  }
+
+  void set_flory(int a, int b, double chi) {
+    if (a == b) throw PFError(E_ARG, "AssertionError: alpha != beta");
+    if (!monomers.count(a) || !monomers.count(b))
+      throw PFError(E_ARG, "Interaction contains monomer not present in system.");
+    chis[{std::min(a, b), std::max(a, b)}] = chi;
+  }
+
+  void set_cell(int dim, const std::string& crystal, const std::vector<double>& params) {
+    const int nd = (nx > 1) + (ny > 1) + (nz > 1);
+    if (dim != nd) throw PFError(E_ARG, "Number of non-singleton dimensions in System and Cell do not match!");
+    const int npr = crystal_nparams(dim, crystal);
+    if (npr < 0) throw PFError(E_ARG, "Unrecognized crystal system `" + crystal + "` for dim = " + std::to_string(dim) + ".");
+    if ((int)params.size() != npr) throw PFError(E_ARG, "AssertionError: wrong number of cell parameters");
+    cell.dim = dim;
+    cell.crystal = crystal;
+    cell.params = params;
+    cell.update();
+    has_cell = true;
+    ++cell_version;
+  }
+
+  void cell_update() {
+    cell.update();
+    ++cell_version;
+  }
+
+  void require_ready() {
+    if (!has_cell) throw PFError(E_STATE, "no unit cell set");
+    if (species.empty()) throw PFError(E_STATE, "no species added");
+  }
+
+  // ---------------------------------------------------------------- propagator setup
+  template <typename T>
+  void ensure_prop(int p) {
+    if (!jobs_dirty[p]) return;
+    std::vector<ChainJob<T>> hjobs;
+    maxsteps = 0;
+    for (auto& spp : species) {
+      Species& sp = *spp;
+      if (sp.kind != 0) continue;
+      const int nb = sp.nblocks();
+      sp.q[p].alloc(sizeof(T) * (size_t)(sp.Ns + 1) * ng);
+      if (nb > 1) sp.qc[p].alloc(sizeof(T) * (size_t)(sp.Ns + 1) * ng);
+      sp.lw[p].clear();
+      sp.ld[p].clear();
+      for (int b = 0; b < nb; ++b) {
+        sp.lw[p].emplace_back(new DevBuf());
+        sp.lw[p].back()->alloc(sizeof(T) * ng);
+        sp.ld[p].emplace_back(new DevBuf());
+        sp.ld[p].back()->alloc(sizeof(T) * nk);
+      }
+      sp.ld_version[p] = -1;
+      // step operators: forward step t (s = t -> t+1) in block b with bgn0 <= t < end0,
+      // backward step t (s = Ns-t -> Ns-t-1) in block b with bgn0 < Ns-t <= end0
+      std::vector<StepOp<T>> hops(2 * (size_t)sp.Ns);
+      for (int t = 0; t < sp.Ns; ++t) {
+        for (int b = 0; b < nb; ++b) {
+          const int b0 = sp.begin_block[b] - 1, b1 = sp.begin_block[b + 1] - 1;
+          if (b0 <= t && t < b1) hops[t] = StepOp<T>{sp.lw[p][b]->as<T>(), sp.ld[p][b]->as<T>()};
+          const int s = sp.Ns - t;
+          if (b0 < s && s <= b1) hops[sp.Ns + t] = StepOp<T>{sp.lw[p][b]->as<T>(), sp.ld[p][b]->as<T>()};
+        }
+      }
+      sp.ops[p].alloc(sizeof(StepOp<T>) * hops.size());
+      PF_CU(cudaMemcpy(sp.ops[p].p, hops.data(), sizeof(StepOp<T>) * hops.size(), cudaMemcpyHostToDevice));
+      const StepOp<T>* ops = sp.ops[p].as<StepOp<T>>();
+      Cx<T>* kb0 = nullptr;
+      Cx<T>* kb1 = nullptr;
+      if (nz > 1) {
+        sp.kbuf[p][0].alloc(sizeof(Cx<T>) * nk);
+        kb0 = sp.kbuf[p][0].as<Cx<T>>();
+        if (nb > 1) {
+          sp.kbuf[p][1].alloc(sizeof(Cx<T>) * nk);
+          kb1 = sp.kbuf[p][1].as<Cx<T>>();
+        }
+      }
+      hjobs.push_back(ChainJob<T>{sp.q[p].as<T>(), ops, kb0, 0, +1, sp.Ns, 0});
+      if (nb > 1) hjobs.push_back(ChainJob<T>{sp.qc[p].as<T>(), ops + sp.Ns, kb1, sp.Ns, -1, sp.Ns, 0});
+      maxsteps = std::max(maxsteps, sp.Ns);
+    }
+    njobs = (int)hjobs.size();
+    jobs[p].alloc(sizeof(ChainJob<T>) * std::max(1, njobs));
+    if (njobs) PF_CU(cudaMemcpy(jobs[p].p, hjobs.data(), sizeof(ChainJob<T>) * njobs, cudaMemcpyHostToDevice));
+    jobs_dirty[p] = false;
+  }
+
+  // ---------------------------------------------------------------- density!(sys)
+  template <typename T>
+  void density_t(int p) {
+    require_ready();
+    ensure_prop<T>(p);
+    const double invng = 1.0 / (double)ng;
+    PF_CU(cudaMemsetAsync(rho.p, 0, sizeof(double) * ng * nmon(), st));
+    if (timing) PF_CU(cudaEventRecord(ev[0], st));
+    const CellGeom g = geom();
+    mde_steps = 0;
+    for (auto& spp : species) {
+      Species& sp = *spp;
+      if (sp.kind != 0) continue;
+      for (int b = 0; b < sp.nblocks(); ++b) {
+        const auto& m = monomers.at(sp.mid_block[b]);
+        launch_lw<T>(sp.lw[p][b]->as<T>(), grid_ptr(w, sp.mid_block[b]), sp.ds_block[b] / 2.0 * m.first, ng, st);
+        if (sp.ld_version[p] != cell_version)
+          launch_ld<T>(sp.ld[p][b]->as<T>(), g, sp.ds_block[b] * sp.b_block[b] * sp.b_block[b] / 6.0, invng, nk, st);
+      }
+      sp.ld_version[p] = cell_version;
+      launch_fill<T>(sp.q[p].as<T>(), (T)1, ng, st);
+      if (sp.nblocks() > 1) launch_fill<T>(sp.qc[p].as<T>() + (long)sp.Ns * ng, (T)1, ng, st);
+      mde_steps += sp.Ns * (sp.nblocks() > 1 ? 2 : 1);
+    }
+    check_launch();
+    if (timing) PF_CU(cudaEventRecord(ev[1], st));
+    if (njobs) launch_chains<T>(jobs[p].as<ChainJob<T>>(), njobs, maxsteps, GridDims{nx, ny, nz}, tw<T>(p), st);
+    check_launch();
+    if (timing) PF_CU(cudaEventRecord(ev[2], st));
+    for (auto& spp : species) {
+      Species& sp = *spp;
+      if (sp.kind == 0) {
+        launch_sum<T>(sp.q[p].as<T>() + (long)sp.Ns * ng, ng, part.as<double>(), sp.Qdev.as<double>(), (double)ng, st);
+        SimpsonBlocks sb{};
+        sb.nblocks = sp.nblocks();
+        for (int b = 0; b < sb.nblocks; ++b) {
+          sb.mon[b] = mon_index(sp.mid_block[b]);
+          sb.bgn[b] = sp.begin_block[b] - 1;
+          sb.end[b] = sp.begin_block[b + 1] - 1;
+          sb.ds[b] = sp.ds_block[b];
+        }
+        const T* qc = sp.nblocks() > 1 ? sp.qc[p].as<T>() : nullptr;
+        launch_simpson<T>(rho.as<double>(), sp.q[p].as<T>(), qc, sp.nblocks() == 1, sp.Ns, ng, sb, sp.phi, sp.Nref,
+                          sp.Qdev.as<double>(), st);
+      } else {
+        const int mid = sp.mids[0];
+        const double vol = monomers.at(mid).first;
+        launch_point_q(grid_ptr(w, mid), vol, ng, part.as<double>(), sp.Qdev.as<double>(), st);
+        launch_point_density(grid_ptr(rho, mid), grid_ptr(w, mid), vol, sp.phi, sp.Qdev.as<double>(), ng, st);
+      }
+      sp.Q_valid = false;
+    }
+    check_launch();
+    if (timing) {
+      PF_CU(cudaEventRecord(ev[3], st));
+      PF_CU(cudaEventSynchronize(ev[3]));
+      float a = 0, b = 0;
+      PF_CU(cudaEventElapsedTime(&a, ev[1], ev[2]));
+      PF_CU(cudaEventElapsedTime(&b, ev[0], ev[3]));
+      t_prop_ms = a;
+      t_dens_ms = b;
+    }
+    last_prec = p;
+  }
+  void density() {
+    if (prec == 0) density_t<double>(0);
+    else density_t<float>(1);
+  }
+
+  void fetch_Q() {
+    for (auto& sp : species) {
+      if (!sp->Q_valid) {
+        PF_CU(cudaMemcpyAsync(&sp->Q, sp->Qdev.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+      }
+    }
+    PF_CU(cudaStreamSynchronize(st));
+    for (auto& sp : species) {
+      sp->Q_valid = true;
+      sp->mu = std::log(sp->phi / sp->Q);  // muphi! canonical (system.jl:248-259)
+    }
+  }
+
+  // ---------------------------------------------------------------- residuals!(sys)
+  void residuals() {
+    density();
+    launch_residuals(w.as<double>(), pot.as<double>(), res.as<double>(), rho.as<double>(), monomer_set(), ng, true,
+                     part.as<double>(), sums.as<double>(), st);
+    check_launch();
+  }
+
+  // field_error and free_energy from one reduction pass
+  void stats(double& ferr, double& fhelm) {
+    launch_stats(w.as<double>(), res.as<double>(), rho.as<double>(), monomer_set(), ng, part.as<double>(),
+                 stats4.as<double>(), st);
+    check_launch();
+    double s[4];
+    PF_CU(cudaMemcpyAsync(s, stats4.p, sizeof(s), cudaMemcpyDeviceToHost, st));
+    PF_CU(cudaStreamSynchronize(st));
+    ferr = std::sqrt(s[0]) / std::sqrt(2.220446049250313e-16 + s[1]);
+    double ftrans = 0.0;
+    for (auto& sp : species) {
+      const double phi = sp->phi, mu = sp->phi;  // quirk Q3 (system.jl:407)
+      if (phi > 1e-8) ftrans += phi * (mu - 1.0) / sp->Nref;
+    }
+    double ffield = -s[2];
+    ffield /= (double)ng;
+    fhelm = ftrans + ffield + s[3] / (double)ng;
+  }
+
+  double free_energy_bulk() {
+    std::map<int, double> fr;
+    for (int id : mon_ids) fr[id] = 0.0;
+    double f = 0.0;
+    for (auto& sp : species) {
+      if (sp->phi > 1e-8) f += sp->phi * (std::log(sp->phi) - 1.0) / sp->Nref;
+      for (int mid : sp->mids) fr[mid] += sp->phi * sp->monomer_fraction(mid);
+    }
+    double e = 0.0;
+    for (auto& kv : chis) {
+      const double va = monomers.at(kv.first.first).first, vb = monomers.at(kv.first.second).first;
+      e += kv.second * (fr[kv.first.first] / va) * (fr[kv.first.second] / vb);
+    }
+    return f + e;
+  }
+
+  void validate() {  // system.jl:192-237
+    require_ready();
+    // fields initialised: some field with nonzero mean or std
+    launch_stats(w.as<double>(), w.as<double>(), w.as<double>(), monomer_set(), ng, part.as<double>(),
+                 stats4.as<double>(), st);
+    check_launch();
+    double s[4];
+    PF_CU(cudaMemcpyAsync(s, stats4.p, sizeof(s), cudaMemcpyDeviceToHost, st));
+    PF_CU(cudaStreamSynchronize(st));
+    if (s[1] == 0.0) throw PFError(E_ARG, "Fields must be initialized before SCFT simulation.");
+    double phisum = 0.0;
+    for (auto& sp : species) phisum += sp->phi;
+    if (!isapprox(phisum, 1.0)) throw PFError(E_ARG, "Species volume fractions do not sum to unity.");
+    double charge = 0.0;
+    for (int id : mon_ids) {
+      double fr = 0.0;
+      for (auto& sp : species) fr += sp->phi * sp->monomer_fraction(id);
+      charge += fr * monomers.at(id).second / monomers.at(id).first;
+    }
+    if (!(charge == 0.0)) throw PFError(E_ARG, "Bulk system not charge neutral.");
+    for (int id : mon_ids) {
+      bool found = false;
+      for (auto& sp : species)
+        if (std::find(sp->mids.begin(), sp->mids.end(), id) != sp->mids.end()) found = true;
+      if (!found) throw PFError(E_ARG, "Monomer with ID = " + std::to_string(id) + " not found in any species.");
+    }
+  }
+
+  // ---------------------------------------------------------------- scfstress(sys)
+  template <typename T>
+  std::vector<double> chain_dQ(Species& sp, int p) {
+    const int npr = cell.np();
+    std::vector<double> dQ(npr, 0.0);
+    struct It { const T* q; const T* qc; double w; double b; };
+    std::vector<It> items;
+    for (int b = 0; b < sp.nblocks(); ++b) {
+      const int bgn = sp.begin_block[b], end = sp.begin_block[b + 1];
+      for (int s = bgn; s <= end; ++s) {
+        double ds = sp.ds_block[b];
+        if (s != bgn && s != end) ds *= (s % 2 == 0) ? 4.0 : 2.0;
+        const long s0 = s - 1;
+        const T* q = sp.q[p].as<T>() + s0 * ng;
+        const T* qc = sp.nblocks() > 1 ? sp.qc[p].as<T>() + s0 * ng : sp.q[p].as<T>() + (sp.Ns - s0) * ng;
+        items.push_back(It{q, qc, ds, sp.b_block[b]});
+      }
+    }
+    const int nit = (int)items.size();
+    std::vector<double> qint(nit * (size_t)npr, 0.0);
+    const GridDims d{nx, ny, nz};
+    if (nz == 1) {
+      std::vector<StressItem<T>> h(nit);
+      for (int i = 0; i < nit; ++i) h[i] = StressItem<T>{items[i].q, items[i].qc};
+      DevBuf di, dp;
+      di.alloc(sizeof(StressItem<T>) * nit);
+      dp.alloc(sizeof(double) * nit * npr);
+      PF_CU(cudaMemcpyAsync(di.p, h.data(), di.bytes, cudaMemcpyHostToDevice, st));
+      launch_stress<T>(di.as<StressItem<T>>(), nit, nullptr, nullptr, nullptr, nullptr, d, dksq.as<double>(), npr,
+                       dp.as<double>(), tw<T>(p), st);
+      check_launch();
+      PF_CU(cudaMemcpyAsync(qint.data(), dp.p, dp.bytes, cudaMemcpyDeviceToHost, st));
+      PF_CU(cudaStreamSynchronize(st));
+    } else {
+      const int M = zM(p);
+      const int nkp = (nx / 2 + 1) * ny;
+      const int ntiles = (nkp + M - 1) / M;
+      const int chunk = 16;
+      DevBuf kq, kqc, ptrs, dp;
+      kq.alloc(sizeof(Cx<T>) * nk * chunk);
+      kqc.alloc(sizeof(Cx<T>) * nk * chunk);
+      ptrs.alloc(sizeof(void*) * 4 * chunk);
+      dp.alloc(sizeof(double) * (size_t)chunk * ntiles * npr);
+      std::vector<double> hp((size_t)chunk * ntiles * npr);
+      for (int c0 = 0; c0 < nit; c0 += chunk) {
+        const int cn_ = std::min(chunk, nit - c0);
+        std::vector<void*> hptr(4 * chunk);
+        for (int i = 0; i < cn_; ++i) {
+          hptr[i] = (void*)items[c0 + i].q;
+          hptr[chunk + i] = (void*)items[c0 + i].qc;
+          hptr[2 * chunk + i] = (void*)(kq.as<Cx<T>>() + (long)i * nk);
+          hptr[3 * chunk + i] = (void*)(kqc.as<Cx<T>>() + (long)i * nk);
+        }
+        PF_CU(cudaMemcpyAsync(ptrs.p, hptr.data(), sizeof(void*) * 4 * chunk, cudaMemcpyHostToDevice, st));
+        void** pp = ptrs.as<void*>();
+        launch_stress<T>(nullptr, cn_, (const T* const*)pp, (const T* const*)(pp + chunk),
+                         (Cx<T>* const*)(pp + 2 * chunk), (Cx<T>* const*)(pp + 3 * chunk), d, dksq.as<double>(), npr,
+                         dp.as<double>(), tw<T>(p), st);
+        check_launch();
+        PF_CU(cudaMemcpyAsync(hp.data(), dp.p, sizeof(double) * (size_t)cn_ * ntiles * npr, cudaMemcpyDeviceToHost, st));
+        PF_CU(cudaStreamSynchronize(st));
+        for (int i = 0; i < cn_; ++i)
+          for (int k = 0; k < npr; ++k) {
+            double s = 0.0;
+            for (int t = 0; t < ntiles; ++t) s += hp[((size_t)i * ntiles + t) * npr + k];
+            qint[(size_t)(c0 + i) * npr + k] = s;
+          }
+      }
+    }
+    const double ng2 = (double)ng * (double)ng;
+    for (int i = 0; i < nit; ++i)
+      for (int k = 0; k < npr; ++k)
+        dQ[k] -= items[i].b * items[i].b * items[i].w * qint[(size_t)i * npr + k] / 6.0 / ng2;
+    for (int k = 0; k < npr; ++k) {
+      dQ[k] /= 3.0;
+      dQ[k] /= sp.Q * sp.Nref;
+    }
+    return dQ;
+  }
+
+  std::vector<double> scfstress() {
+    require_ready();
+    if (last_prec < 0) throw PFError(E_STATE, "scfstress needs a density solve first");
+    const int npr = cell.np();
+    if (dksq_version != cell_version) {
+      dksq.alloc(sizeof(double) * nk * std::max(1, npr));
+      launch_dksq(dksq.as<double>(), geom(), npr, nk, st);
+      check_launch();
+      dksq_version = cell_version;
+    }
+    fetch_Q();
+    std::vector<double> stress(npr, 0.0);
+    for (auto& sp : species) {
+      if (sp->kind != 0) continue;
+      std::vector<double> dQ = last_prec == 0 ? chain_dQ<double>(*sp, 0) : chain_dQ<float>(*sp, 1);
+      for (int k = 0; k < npr; ++k) stress[k] -= sp->phi * dQ[k];
+    }
+    return stress;
+  }
+
+  // ---------------------------------------------------------------- Anderson (anderson.jl)
+  double* hist_slot(DevBuf& b, int logical) {
+    const int nslot = and_.nhist + 1;
+    const int phys = (and_.base + logical) % nslot;
+    return b.as<double>() + (long)phys * nmon() * ng;
+  }
+
+  void anderson_setup() {  // anderson.jl:54-92
+    if (!and_.exists) throw PFError(E_STATE, "no AndersonUpdater created");
+    if (and_.is_setup) {
+      fprintf(stderr, "Warning: Using previous iterations in AndersonUpdater history.\n");
+      return;
+    }
+    const size_t slot = sizeof(double) * nmon() * ng;
+    and_.res_hist.alloc(slot * (and_.nhist + 1));
+    and_.field_hist.alloc(slot * (and_.nhist + 1));
+    PF_CU(cudaMemsetAsync(and_.res_hist.p, 0, and_.res_hist.bytes, st));
+    PF_CU(cudaMemsetAsync(and_.field_hist.p, 0, and_.field_hist.bytes, st));
+    and_.base = 0;
+    PF_CU(cudaMemcpyAsync(hist_slot(and_.field_hist, 0), w.p, slot, cudaMemcpyDeviceToDevice, st));
+    and_.iter = 0;
+    and_.iter_hist = 0;
+    and_.lam = 0.0;
+    and_.is_setup = true;
+  }
+
+  void anderson_step() {  // anderson.jl:98-228
+    if (!and_.is_setup) throw PFError(E_STATE, "AndersonUpdater not set up");
+    auto& A = and_;
+    A.iter += 1;
+    if (A.iter < A.nhist + 1) {
+      A.iter_hist = A.iter - 1;
+      A.lam = 1.0 - std::pow(0.9, A.iter);
+    } else {
+      A.iter_hist = A.nhist;
+      A.lam = 1.0;
+    }
+    const int it = A.iter, ih = A.iter_hist;
+    const long nall = (long)nmon() * ng;
+    residuals();
+    PF_CU(cudaMemcpyAsync(hist_slot(A.res_hist, ih), res.p, sizeof(double) * nall, cudaMemcpyDeviceToDevice, st));
+    if (it <= A.iter_euler) {
+      launch_axpy(w.as<double>(), res.as<double>(), A.lam_euler, nall, st);
+    } else {
+      HistPtrs h{};
+      for (int j = 0; j <= ih; ++j) {
+        h.res[j] = hist_slot(A.res_hist, j);
+        h.field[j] = hist_slot(A.field_hist, j);
+      }
+      launch_gram(h, ih, nall, part.as<double>(), packed.as<double>(), st);
+      launch_solve(packed.as<double>(), ih, cn.as<double>(), status.as<int>(), st);
+      check_launch();
+      int sv = 0;
+      PF_CU(cudaMemcpyAsync(&sv, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+      PF_CU(cudaStreamSynchronize(st));
+      if (sv != 0)
+        throw PFError(E_SINGULAR, "Error inverting Umn matrix on iteration " + std::to_string(it) +
+                                      ": SingularException(" + std::to_string(sv) + ")");
+      launch_mix(w.as<double>(), h, ih, cn.as<double>(), A.lam, nall, st);
+    }
+    check_launch();
+    if (it < A.nhist + 1) {
+      PF_CU(cudaMemcpyAsync(hist_slot(A.field_hist, it), w.p, sizeof(double) * nall, cudaMemcpyDeviceToDevice, st));
+    } else {
+      A.base = (A.base + 1) % (A.nhist + 1);
+      PF_CU(cudaMemcpyAsync(hist_slot(A.field_hist, A.nhist), w.p, sizeof(double) * nall, cudaMemcpyDeviceToDevice, st));
+    }
+  }
+
+  // ---------------------------------------------------------------- Domain (domain.jl)
+  double stress_error() const {
+    double s = 0.0;
+    for (double v : dom.stress) s += v * v;
+    return std::sqrt(s);
+  }
+  void domain_setup() {
+    if (!dom.exists) throw PFError(E_STATE, "no DomainUpdater created");
+    const int npr = cell.np();
+    dom.stress = scfstress();
+    dom.oldparams.assign(npr, 0.0);
+    dom.step.assign(npr, 0.0);
+    dom.dstress.assign(npr * npr, 0.0);
+    dom.is_setup = true;
+  }
+  // FD step of the Jacobian: the reference's 1e-8 (domain.jl:101) for FP64 propagators; in
+  // FP32 the stress carries ~1e-7 relative noise, so the FP32 phase of a mixed run uses 1e-4.
+  double fd_dx() const { return prec == 0 ? 1e-8 : 1e-4; }
+  void dstress_update() {  // domain.jl:94-121
+    const int npr = cell.np();
+    dom.oldparams = cell.params;
+    const double dx = fd_dx();
+    const double x = 1.0 / dx;
+    for (int k = 0; k < npr; ++k) {
+      cell.params = dom.oldparams;
+      cell.params[k] += dx;
+      cell_update();
+      density();
+      std::vector<double> ps = scfstress();
+      for (int i = 0; i < npr; ++i) dom.dstress[i * npr + k] = x * (ps[i] - dom.stress[i]);
+    }
+    cell.params = dom.oldparams;
+    // The reference re-runs density! here with the stale perturbed cell (quirk Q4).  Its
+    // result is overwritten by the residuals! that follows the Newton step before anything
+    // reads it, so the solve is skipped.
+  }
+  void domain_step(int nsteps, bool stress_current) {  // domain.jl:50-92
+    if (!dom.is_setup) throw PFError(E_STATE, "DomainUpdater not set up");
+    const int npr = cell.np();
+    if (!stress_current) dom.stress = scfstress();
+    for (int iter = 0; iter < nsteps; ++iter) {
+      dstress_update();
+      if (cell.dim == 1) {
+        for (int k = 0; k < npr; ++k) dom.step[k] = -1.0 * dom.stress[0] / dom.dstress[0];
+      } else {
+        std::vector<double> inv;
+        if (!lu_inverse(dom.dstress, npr, inv)) throw PFError(E_SINGULAR, "SingularException in DomainUpdater");
+        for (int i = 0; i < npr; ++i) {
+          double s = 0.0;
+          for (int j = 0; j < npr; ++j) s += inv[i * npr + j] * dom.stress[j];
+          dom.step[i] = -1.0 * s;
+        }
+      }
+      double ss = 0.0;
+      for (double v : dom.step) ss += v * v;
+      const double step_size = std::sqrt(ss);
+      if (step_size > dom.pmax)
+        for (double& v : dom.step) v *= dom.pmax / step_size;
+      for (int k = 0; k < npr; ++k) {
+        cell.params[k] += dom.lam * dom.step[k];
+        cell.params[k] = dom.rlxn * cell.params[k] + (1 - dom.rlxn) * dom.oldparams[k];
+      }
+      cell_update();
+      // density!(sys) directly followed by residuals!(sys) recomputes the same density
+      // twice in the reference; one solve gives the identical state.
+      residuals();
+      dom.stress = scfstress();
+    }
+  }
+
+  // ---------------------------------------------------------------- scft! (simulate.jl:60-148)
+  static bool isconverged(double ferr, double ftol, double serr, double stol, bool vcell) {
+    bool fc = false, sc = true;
+    if (ferr < ftol) {
+      fc = true;
+      if (vcell && serr > stol) sc = false;
+    }
+    return fc && sc;
+  }
+
+  pf_scft_results scft(const pf_scft_options& o, bool vcell) {
+    auto t0 = std::chrono::steady_clock::now();
+    pf_scft_results r{};
+    r.switch_step = -1;
+    if (!and_.exists) throw PFError(E_STATE, "no AndersonUpdater created");
+    if (vcell && !dom.exists) throw PFError(E_STATE, "no DomainUpdater created");
+    validate();
+    residuals();
+    anderson_setup();
+    int step = 0;
+    double ferr, fhelm;
+    stats(ferr, fhelm);
+    double serr = 0.0;
+    if (vcell) {
+      domain_setup();
+      serr = stress_error();
+    }
+    bool converged = isconverged(ferr, o.ftol, serr, o.stol, vcell);
+    const bool mixed = o.mixed_switch_ferr > 0.0 && prec == 1;
+    if (mixed && ferr < o.mixed_switch_ferr) {
+      prec = 0;
+      r.switch_step = 0;
+    }
+    if (!converged && o.nsout > 0) printf("--------------------------------------------------------------\n");
+    while (step < o.nsteps && !converged) {
+      if (o.nsout > 0 && step % o.nsout == 0)
+        printf("Step (%-5d / %5d): ferr = %8e, fhelm = %.5e\n", step, o.nsteps, ferr, fhelm);
+      anderson_step();
+      if (vcell && step % dom.nskip == 0) {
+        dom.stress = scfstress();
+        serr = stress_error();
+        if (serr > o.stol) {
+          domain_step(dom.nper, true);
+          serr = stress_error();
+          if (o.nsout > 0) printf("Updating cell dimensions: serr = %.5e\n", serr);
+        }
+      }
+      stats(ferr, fhelm);
+      if (std::isnan(ferr)) throw PFError(E_NAN, "Diverging field updater -- breaking.");
+      converged = isconverged(ferr, o.ftol, serr, o.stol, vcell);
+      if (converged) {
+        if (o.nsout > 0) printf("Converged @ step = %d: ferr = %8e, fhelm = %.5e\n", step, ferr, fhelm);
+        break;
+      }
+      if (mixed && prec == 1 && ferr < o.mixed_switch_ferr) {
+        prec = 0;
+        r.switch_step = step;
+      }
+      step += 1;
+    }
+    residuals();
+    stats(ferr, fhelm);
+    if (vcell) serr = stress_error();
+    r.time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    r.nsteps = step;
+    r.converged = converged ? 1 : 0;
+    r.ferr = ferr;
+    r.serr = serr;
+    r.fhelm = fhelm;
+    return r;
+  }
+
+  // ---------------------------------------------------------------- low-level propagate
+  template <typename T>
+  void propagate_t(int p, const double* omega, double vol, double b, double ds, const double* qin, double* qout,
+                   int nsteps) {
+    if (!has_cell) throw PFError(E_STATE, "no unit cell set");
+    if (nsteps < 1) throw PFError(E_ARG, "nsteps must be positive");
+    DevBuf dw, lw, ld, hist, ops, job, kb;
+    dw.alloc(sizeof(double) * ng);
+    lw.alloc(sizeof(T) * ng);
+    ld.alloc(sizeof(T) * nk);
+    hist.alloc(sizeof(T) * ng * (nsteps + 1));
+    PF_CU(cudaMemcpyAsync(dw.p, omega, sizeof(double) * ng, cudaMemcpyHostToDevice, st));
+    launch_lw<T>(lw.as<T>(), dw.as<double>(), ds / 2.0 * vol, ng, st);
+    launch_ld<T>(ld.as<T>(), geom(), ds * b * b / 6.0, 1.0 / (double)ng, nk, st);
+    std::vector<T> h0(ng);
+    for (long i = 0; i < ng; ++i) h0[i] = (T)qin[i];
+    PF_CU(cudaMemcpyAsync(hist.p, h0.data(), sizeof(T) * ng, cudaMemcpyHostToDevice, st));
+    std::vector<StepOp<T>> hops(nsteps, StepOp<T>{lw.as<T>(), ld.as<T>()});
+    ops.alloc(sizeof(StepOp<T>) * nsteps);
+    PF_CU(cudaMemcpyAsync(ops.p, hops.data(), ops.bytes, cudaMemcpyHostToDevice, st));
+    Cx<T>* kp = nullptr;
+    if (nz > 1) {
+      kb.alloc(sizeof(Cx<T>) * nk);
+      kp = kb.as<Cx<T>>();
+    }
+    ChainJob<T> hj{hist.as<T>(), ops.as<StepOp<T>>(), kp, 0, +1, nsteps, 0};
+    job.alloc(sizeof(hj));
+    PF_CU(cudaMemcpyAsync(job.p, &hj, sizeof(hj), cudaMemcpyHostToDevice, st));
+    launch_chains<T>(job.as<ChainJob<T>>(), 1, nsteps, GridDims{nx, ny, nz}, tw<T>(p), st);
+    check_launch();
+    std::vector<T> ho(ng);
+    PF_CU(cudaMemcpyAsync(ho.data(), hist.as<T>() + (long)nsteps * ng, sizeof(T) * ng, cudaMemcpyDeviceToHost, st));
+    PF_CU(cudaStreamSynchronize(st));
+    for (long i = 0; i < ng; ++i) qout[i] = (double)ho[i];
+  }
+};
+
+// Grids with kernels: planes (Nx, Ny) of 1D rows Nx in {8, 16, 32, 48, 64, 96, 128, 256},
+// squares Nx = Ny in {16, ..., 128} and 2:1 rectangles; Nz = 1 or a supported length.
+static bool dims_supported(int nx, int ny, int nz, std::string& why) {
+  if (!shape_supported<double>(nx, ny, nz) || !shape_supported<float>(nx, ny, nz)) {
+    why = "grid " + std::to_string(nx) + "x" + std::to_string(ny) + "x" + std::to_string(nz) + " has no kernels";
+    return false;
+  }
+  return true;
+}
+
+}  // namespace pf
+
+// ====================================================================== C ABI
+struct pf_system {
+  std::unique_ptr<pf::System> s;
+  std::string err;
+};
+
+namespace {
+template <typename F>
+int guard(pf_system* h, F&& f) {
+  if (!h || !h->s) return PF_EARG;
+  try {
+    f(*h->s);
+    h->err.clear();
+    return PF_OK;
+  } catch (const pf::PFError& e) {
+    h->err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    h->err = e.what();
+    return PF_EARG;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int pf_version(void) { return 100; }
+
+const char* pf_status_string(int status) {
+  switch (status) {
+    case PF_OK: return "ok";
+    case PF_EARG: return "invalid argument";
+    case PF_ECUDA: return "CUDA error";
+    case PF_ENAN: return "Diverging field updater -- breaking.";
+    case PF_ESINGULAR: return "Error inverting Umn matrix";
+    case PF_ETIMEOUT: return "device wait timed out";
+    case PF_ESTATE: return "call out of order";
+    case PF_ENOMEM: return "device allocation failed";
+    case PF_EUNSUPPORTED: return "unsupported grid size";
+    default: return "unknown status";
+  }
+}
+
+int pf_system_create(pf_system** out, int nx, int ny, int nz, int precision) {
+  if (!out) return PF_EARG;
+  *out = nullptr;
+  if (!(nx >= ny && ny >= nz && nz >= 1)) return PF_EARG;  // descending dims (system.jl:58)
+  if (precision != PF_FP64 && precision != PF_FP32) return PF_EARG;
+  std::string why;
+  if (!pf::dims_supported(nx, ny, nz, why)) return PF_EUNSUPPORTED;
+  auto* h = new pf_system();
+  try {
+    h->s.reset(new pf::System(nx, ny, nz, precision));
+  } catch (const pf::PFError& e) {
+    delete h;
+    return e.code;
+  }
+  *out = h;
+  return PF_OK;
+}
+
+int pf_system_destroy(pf_system* sys) {
+  delete sys;
+  return PF_OK;
+}
+
+const char* pf_last_error(const pf_system* sys) { return sys ? sys->err.c_str() : "null handle"; }
+
+int pf_set_precision(pf_system* sys, int precision) {
+  return guard(sys, [&](pf::System& s) {
+    if (precision != PF_FP64 && precision != PF_FP32) throw pf::PFError(PF_EARG, "precision must be PF_FP64 or PF_FP32");
+    s.prec = precision;
+  });
+}
+
+int pf_get_precision(const pf_system* sys, int* precision) {
+  if (!sys || !precision) return PF_EARG;
+  *precision = sys->s->prec;
+  return PF_OK;
+}
+
+int pf_set_cell(pf_system* sys, int dim, const char* crystal, const double* params, int nparams) {
+  return guard(sys, [&](pf::System& s) {
+    if (!crystal || (nparams > 0 && !params) || nparams < 0 || nparams > pf::kMaxParams)
+      throw pf::PFError(PF_EARG, "bad cell arguments");
+    std::string c(crystal);
+    if (!c.empty() && c[0] == ':') c = c.substr(1);
+    s.set_cell(dim, c, std::vector<double>(params, params + nparams));
+  });
+}
+
+int pf_get_cell(const pf_system* sys, double* params, int nparams, double* volume) {
+  if (!sys || !sys->s->has_cell) return PF_ESTATE;
+  const auto& c = sys->s->cell;
+  if (params)
+    for (int i = 0; i < std::min(nparams, c.np()); ++i) params[i] = c.params[i];
+  if (volume) *volume = c.volume;
+  return PF_OK;
+}
+
+int pf_get_basis(const pf_system* sys, double* R, double* G) {
+  if (!sys || !sys->s->has_cell) return PF_ESTATE;
+  for (int i = 0; i < 9; ++i) {
+    if (R) R[i] = sys->s->cell.R[i];
+    if (G) G[i] = sys->s->cell.G[i];
+  }
+  return PF_OK;
+}
+
+int pf_add_monomer(pf_system* sys, int id, double vol, double charge) {
+  return guard(sys, [&](pf::System& s) { s.add_monomer(id, vol, charge); });
+}
+
+int pf_add_multiblock(pf_system* sys, int nblocks, const int* block_mids, const int* N_block, const double* b_block,
+                      int Ns, double phi) {
+  return guard(sys, [&](pf::System& s) {
+    if (!block_mids || !N_block || !b_block) throw pf::PFError(PF_EARG, "null block arrays");
+    s.add_multiblock(nblocks, block_mids, N_block, b_block, Ns, phi);
+  });
+}
+
+int pf_add_point(pf_system* sys, int mid, double phi) {
+  return guard(sys, [&](pf::System& s) { s.add_point(mid, phi); });
+}
+
+int pf_set_flory(pf_system* sys, int a, int b, double chi) {
+  return guard(sys, [&](pf::System& s) { s.set_flory(a, b, chi); });
+}
+
+int pf_species_info(const pf_system* sys, int isp, int* Ns, double* Nref, int* begin_block, double* ds_block,
+                    int max_blocks) {
+  if (!sys || isp < 0 || isp >= (int)sys->s->species.size()) return PF_EARG;
+  const auto& sp = *sys->s->species[isp];
+  if (Ns) *Ns = sp.Ns;
+  if (Nref) *Nref = sp.Nref;
+  for (int i = 0; i < std::min(max_blocks + 1, (int)sp.begin_block.size()); ++i)
+    if (begin_block) begin_block[i] = sp.begin_block[i];
+  for (int i = 0; i < std::min(max_blocks, (int)sp.ds_block.size()); ++i)
+    if (ds_block) ds_block[i] = sp.ds_block[i];
+  return PF_OK;
+}
+
+int pf_set_field(pf_system* sys, int mid, const double* w) {
+  return guard(sys, [&](pf::System& s) {
+    if (!w) throw pf::PFError(PF_EARG, "null field");
+    PF_CU(cudaMemcpyAsync(s.grid_ptr(s.w, mid), w, sizeof(double) * s.ng, cudaMemcpyHostToDevice, s.st));
+    PF_CU(cudaStreamSynchronize(s.st));
+  });
+}
+
+int pf_get_grid(pf_system* sys, int kind, int mid, double* out) {
+  return guard(sys, [&](pf::System& s) {
+    if (!out) throw pf::PFError(PF_EARG, "null output");
+    pf::DevBuf* b = kind == PF_FIELD ? &s.w : kind == PF_DENSITY ? &s.rho : kind == PF_RESIDUAL ? &s.res : &s.pot;
+    PF_CU(cudaMemcpyAsync(out, s.grid_ptr(*b, mid), sizeof(double) * s.ng, cudaMemcpyDeviceToHost, s.st));
+    PF_CU(cudaStreamSynchronize(s.st));
+  });
+}
+
+int pf_get_propagator(pf_system* sys, int isp, int conjugate, int s_idx, double* out) {
+  return guard(sys, [&](pf::System& s) {
+    if (isp < 0 || isp >= (int)s.species.size() || s.species[isp]->kind != 0) throw pf::PFError(PF_EARG, "bad species");
+    auto& sp = *s.species[isp];
+    if (s_idx < 0 || s_idx > sp.Ns || s.last_prec < 0) throw pf::PFError(PF_EARG, "bad contour index / no density");
+    const int p = s.last_prec;
+    long off = (long)s_idx * s.ng;
+    pf::DevBuf* src = &sp.q[p];
+    if (conjugate) {
+      if (sp.nblocks() > 1) src = &sp.qc[p];
+      else off = (long)(sp.Ns - s_idx) * s.ng;
+    }
+    if (p == 0) {
+      PF_CU(cudaMemcpyAsync(out, src->as<double>() + off, sizeof(double) * s.ng, cudaMemcpyDeviceToHost, s.st));
+      PF_CU(cudaStreamSynchronize(s.st));
+    } else {
+      std::vector<float> t(s.ng);
+      PF_CU(cudaMemcpyAsync(t.data(), src->as<float>() + off, sizeof(float) * s.ng, cudaMemcpyDeviceToHost, s.st));
+      PF_CU(cudaStreamSynchronize(s.st));
+      for (long i = 0; i < s.ng; ++i) out[i] = t[i];
+    }
+  });
+}
+
+int pf_validate(pf_system* sys) { return guard(sys, [&](pf::System& s) { s.validate(); }); }
+int pf_density(pf_system* sys) {
+  return guard(sys, [&](pf::System& s) {
+    s.density();
+    PF_CU(cudaStreamSynchronize(s.st));
+  });
+}
+int pf_residuals(pf_system* sys) {
+  return guard(sys, [&](pf::System& s) {
+    s.residuals();
+    PF_CU(cudaStreamSynchronize(s.st));
+  });
+}
+int pf_free_energy(pf_system* sys, double* out) {
+  return guard(sys, [&](pf::System& s) {
+    double fe, fh;
+    s.stats(fe, fh);
+    if (out) *out = fh;
+  });
+}
+int pf_free_energy_bulk(pf_system* sys, double* out) {
+  return guard(sys, [&](pf::System& s) {
+    if (out) *out = s.free_energy_bulk();
+  });
+}
+int pf_field_error(pf_system* sys, double* out) {
+  return guard(sys, [&](pf::System& s) {
+    double fe, fh;
+    s.stats(fe, fh);
+    if (out) *out = fe;
+  });
+}
+int pf_scfstress(pf_system* sys, double* out, int nparams) {
+  return guard(sys, [&](pf::System& s) {
+    std::vector<double> st = s.scfstress();
+    for (int i = 0; i < std::min(nparams, (int)st.size()); ++i) out[i] = st[i];
+  });
+}
+int pf_species_q(pf_system* sys, int isp, double* Q) {
+  return guard(sys, [&](pf::System& s) {
+    if (isp < 0 || isp >= (int)s.species.size()) throw pf::PFError(PF_EARG, "bad species index");
+    s.fetch_Q();
+    if (Q) *Q = s.species[isp]->Q;
+  });
+}
+
+int pf_anderson_create(pf_system* sys, int nhist, int iter_euler, double lam_euler) {
+  return guard(sys, [&](pf::System& s) {
+    if (nhist < 1 || nhist > 60) throw pf::PFError(PF_EARG, "nhist must be in [1, 60]");
+    s.and_.reset();
+    s.and_.exists = true;
+    s.and_.nhist = nhist;
+    s.and_.iter_euler = iter_euler <= 1 ? 1 : iter_euler;
+    s.and_.lam_euler = lam_euler;
+  });
+}
+int pf_anderson_setup(pf_system* sys) { return guard(sys, [&](pf::System& s) { s.anderson_setup(); }); }
+int pf_anderson_step(pf_system* sys) {
+  return guard(sys, [&](pf::System& s) {
+    s.anderson_step();
+    PF_CU(cudaStreamSynchronize(s.st));
+  });
+}
+int pf_domain_create(pf_system* sys, int nper, int nskip, double lam, double pmax, double rlxn) {
+  return guard(sys, [&](pf::System& s) {
+    s.dom = pf::System::Domain();
+    s.dom.exists = true;
+    s.dom.nper = nper;
+    s.dom.nskip = nskip;
+    s.dom.lam = lam;
+    s.dom.pmax = pmax;
+    s.dom.rlxn = rlxn;
+  });
+}
+int pf_domain_setup(pf_system* sys) { return guard(sys, [&](pf::System& s) { s.domain_setup(); }); }
+int pf_domain_step(pf_system* sys, int nsteps) {
+  return guard(sys, [&](pf::System& s) { s.domain_step(nsteps, false); });
+}
+int pf_domain_stress_error(pf_system* sys, double* out) {
+  return guard(sys, [&](pf::System& s) {
+    if (out) *out = s.stress_error();
+  });
+}
+
+int pf_scft(pf_system* sys, const pf_scft_options* opts, int use_domain, pf_scft_results* out) {
+  return guard(sys, [&](pf::System& s) {
+    if (!opts || !out) throw pf::PFError(PF_EARG, "null options/results");
+    *out = s.scft(*opts, use_domain != 0);
+  });
+}
+
+int pf_propagate(pf_system* sys, const double* omega, double vol, double b, double ds, const double* qin, double* qout,
+                 int nsteps) {
+  return guard(sys, [&](pf::System& s) {
+    if (!omega || !qin || !qout) throw pf::PFError(PF_EARG, "null array");
+    if (s.prec == 0) s.propagate_t<double>(0, omega, vol, b, ds, qin, qout, nsteps);
+    else s.propagate_t<float>(1, omega, vol, b, ds, qin, qout, nsteps);
+  });
+}
+
+int pf_set_timing(pf_system* sys, int enable) {
+  return guard(sys, [&](pf::System& s) { s.timing = enable != 0; });
+}
+int pf_last_timing(const pf_system* sys, double* propagate_ms, double* density_ms, int* mde_steps) {
+  if (!sys) return PF_EARG;
+  if (propagate_ms) *propagate_ms = sys->s->t_prop_ms;
+  if (density_ms) *density_ms = sys->s->t_dens_ms;
+  if (mde_steps) *mde_steps = sys->s->mde_steps;
+  return PF_OK;
+}
+int pf_synchronize(pf_system* sys) {
+  return guard(sys, [&](pf::System& s) { PF_CU(cudaStreamSynchronize(s.st)); });
+}
+
+}  // extern "C"

@@ -1,0 +1,440 @@
+// Density integration, field residuals, reductions and Anderson mixing kernels.
+//
+// Reference functions: Simpson density (src/species/multiblock.jl:175-228), point species
+// (src/species/point.jl:36-53), potentials / incompressibility / residuals with mean
+// subtraction (src/system/system.jl:296-340, src/interactions/flory.jl:82-100,
+// src/system/compress.jl:37-61), free energy and field error (system.jl:402-486) and the
+// Anderson Gram matrix, solve and mixed update (src/updaters/anderson.jl:147-205).
+//
+// All system-level grids are FP64: fields w, potentials, residuals and densities are
+// nmon consecutive grids of Ng.  Sums over the grid are deterministic: each CTA writes a
+// partial, a second kernel adds the partials in a fixed order.
+#include "pf_kernels.h"
+
+namespace pf {
+
+static int red_blocks(long n) {
+  long b = (n + 255) / 256;
+  if (b > kRedBlocks) b = kRedBlocks;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+// out[v] = (sum_b part[b * nval + v]) / div
+__global__ void reduce_parts_kernel(const double* __restrict__ part, int nblk, int nval, double* __restrict__ out,
+                                    double div) {
+  __shared__ double red[32];
+  const int v = blockIdx.x;
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc += part[(long)b * nval + v];
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) out[v] = acc / div;
+}
+
+static void reduce_parts(const double* part, int nblk, int nval, double* out, double div, cudaStream_t st) {
+  reduce_parts_kernel<<<nval, 256, 0, st>>>(part, nblk, nval, out, div);
+}
+
+// ------------------------------------------------------------------ plain sums
+template <typename T>
+__global__ void sum_kernel(const T* __restrict__ a, long n, double* __restrict__ part) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    acc += (double)a[i];
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+template <typename T>
+void launch_sum(const T* a, long n, double* part, double* out, double div, cudaStream_t st) {
+  const int nb = red_blocks(n);
+  sum_kernel<T><<<nb, 256, 0, st>>>(a, n, part);
+  reduce_parts(part, nb, 1, out, div, st);
+}
+template void launch_sum<float>(const float*, long, double*, double*, double, cudaStream_t);
+template void launch_sum<double>(const double*, long, double*, double*, double, cudaStream_t);
+
+// ------------------------------------------------------------------ point species
+__global__ void point_q_kernel(const double* __restrict__ w, double vol, long n, double* __restrict__ part) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    acc += exp(-vol * w[i]);
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+void launch_point_q(const double* w, double vol, long n, double* part, double* Qdev, cudaStream_t st) {
+  const int nb = red_blocks(n);
+  point_q_kernel<<<nb, 256, 0, st>>>(w, vol, n, part);
+  reduce_parts(part, nb, 1, Qdev, (double)n, st);
+}
+
+__global__ void point_density_kernel(double* __restrict__ rho, const double* __restrict__ w, double vol, double phi,
+                                     const double* __restrict__ Qdev, long n) {
+  const double Q = *Qdev;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    rho[i] += phi * (exp(-vol * w[i]) / Q);
+}
+
+void launch_point_density(double* rho, const double* w, double vol, double phi, const double* Qdev, long n,
+                          cudaStream_t st) {
+  point_density_kernel<<<red_blocks(n), 256, 0, st>>>(rho, w, vol, phi, Qdev, n);
+}
+
+// ------------------------------------------------------------------ Simpson density
+// rho_all[mon*ng + i] += phi * sum_{blocks of mon} (ds/3) * S_blk(i) / (Q * Nref), with
+// S_blk = q_b qc_b + q_e qc_e + 4 sum_odd q qc + 2 sum_even q qc in the reference's order.
+template <typename T>
+__global__ void simpson_kernel(double* __restrict__ rho_all, const T* __restrict__ q, const T* __restrict__ qc,
+                               bool rev, int Ns, long ng, SimpsonBlocks blk, double phi, double Nref,
+                               const double* __restrict__ Qdev) {
+  const double QN = (*Qdev) * Nref;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ng; i += (long)gridDim.x * blockDim.x) {
+    double bval[kMaxMon * 2];
+    for (int b = 0; b < blk.nblocks; ++b) {
+      const int s0 = blk.bgn[b], s1 = blk.end[b];
+#define PF_QC(s) ((double)(rev ? q[(long)(Ns - (s)) * ng + i] : qc[(long)(s) * ng + i]))
+#define PF_Q(s) ((double)q[(long)(s) * ng + i])
+      double acc = PF_Q(s0) * PF_QC(s0);
+      acc += PF_Q(s1) * PF_QC(s1);
+      for (int s = s0 + 1; s < s1; s += 2) acc += 4.0 * PF_Q(s) * PF_QC(s);
+      for (int s = s0 + 2; s < s1 - 1; s += 2) acc += 2.0 * PF_Q(s) * PF_QC(s);
+#undef PF_QC
+#undef PF_Q
+      bval[b] = (acc * (blk.ds[b] / 3.0)) / QN;
+    }
+    // pool blocks by monomer (block order), then add phi * species density
+    unsigned done = 0;
+    for (int b = 0; b < blk.nblocks; ++b) {
+      const int m = blk.mon[b];
+      if (done & (1u << m)) continue;
+      done |= 1u << m;
+      double dens = 0.0;
+      for (int c = b; c < blk.nblocks; ++c)
+        if (blk.mon[c] == m) dens += bval[c];
+      rho_all[(long)m * ng + i] += phi * dens;
+    }
+  }
+}
+
+template <typename T>
+void launch_simpson(double* rho_all, const T* q, const T* qc, bool qc_reversed, int Ns, long ng,
+                    const SimpsonBlocks& blk, double phi, double Nref, const double* Qdev, cudaStream_t st) {
+  int nb = (int)((ng + 255) / 256);
+  if (nb > 8192) nb = 8192;
+  simpson_kernel<T><<<nb, 256, 0, st>>>(rho_all, q, qc, qc_reversed, Ns, ng, blk, phi, Nref, Qdev);
+}
+template void launch_simpson<float>(double*, const float*, const float*, bool, int, long, const SimpsonBlocks&,
+                                    double, double, const double*, cudaStream_t);
+template void launch_simpson<double>(double*, const double*, const double*, bool, int, long, const SimpsonBlocks&,
+                                     double, double, const double*, cudaStream_t);
+
+// ------------------------------------------------------------------ residuals
+// pot_a = sum_b chi_ab rho_b / v_b ; eta = (sum rho - 1 + sum_a (w_a - pot_a)) / nmon ;
+// res_a = pot_a + eta - w_a.  Partials: sum w_a (v = a), sum res_a (v = nmon + a).
+__global__ void residual_kernel(const double* __restrict__ w, double* __restrict__ pot, double* __restrict__ res,
+                                const double* __restrict__ rho, MonomerSet ms, long ng, double* __restrict__ part) {
+  __shared__ double red[2 * kMaxMon][32];
+  const int nm = ms.nmon;
+  double sw[kMaxMon], sr[kMaxMon];
+  for (int a = 0; a < kMaxMon; ++a) sw[a] = sr[a] = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ng; i += (long)gridDim.x * blockDim.x) {
+    double r[kMaxMon], wv[kMaxMon], p[kMaxMon];
+    double rhosum = 0.0;
+    for (int a = 0; a < nm; ++a) {
+      r[a] = rho[(long)a * ng + i];
+      wv[a] = w[(long)a * ng + i];
+      rhosum += r[a];
+    }
+    double eta = rhosum - 1.0;
+    for (int a = 0; a < nm; ++a) {
+      double pa = 0.0;
+      for (int b = 0; b < nm; ++b) {
+        const double c = ms.chi[a * kMaxMon + b];
+        if (c != 0.0) pa += c * (r[b] / ms.vol[b]);
+      }
+      p[a] = pa;
+      eta += wv[a] - pa;
+    }
+    eta /= (double)nm;
+    for (int a = 0; a < nm; ++a) {
+      const double ra = p[a] + eta - wv[a];
+      pot[(long)a * ng + i] = p[a];
+      res[(long)a * ng + i] = ra;
+      sw[a] += wv[a];
+      sr[a] += ra;
+    }
+  }
+  for (int a = 0; a < nm; ++a) {
+    double v1 = block_sum(sw[a], red[a]);
+    double v2 = block_sum(sr[a], red[kMaxMon + a]);
+    if (threadIdx.x == 0) {
+      part[(long)blockIdx.x * 2 * nm + a] = v1;
+      part[(long)blockIdx.x * 2 * nm + nm + a] = v2;
+    }
+  }
+}
+
+// w_a -= mean(w_a); res_a -= mean(res_a)  (means[a], means[nm + a])
+__global__ void meansub_kernel(double* __restrict__ w, double* __restrict__ res, const double* __restrict__ means,
+                               int nm, long ng) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ng; i += (long)gridDim.x * blockDim.x) {
+    for (int a = 0; a < nm; ++a) {
+      w[(long)a * ng + i] -= means[a];
+      res[(long)a * ng + i] -= means[nm + a];
+    }
+  }
+}
+
+int launch_residuals(double* w, double* pot, double* res, const double* rho, const MonomerSet& ms, long ng,
+                     bool canonical, double* part, double* sums, cudaStream_t st) {
+  const int nb = red_blocks(ng);
+  residual_kernel<<<nb, 256, 0, st>>>(w, pot, res, rho, ms, ng, part);
+  if (canonical) {
+    reduce_parts(part, nb, 2 * ms.nmon, sums, (double)ng, st);
+    meansub_kernel<<<nb, 256, 0, st>>>(w, res, sums, ms.nmon, ng);
+  }
+  return OK;
+}
+
+// ------------------------------------------------------------------ field error / energy sums
+// out4 = { sum res^2, sum w^2, sum rho*w, sum_pairs chi (rho_a/v_a)(rho_b/v_b) }
+__global__ void stats_kernel(const double* __restrict__ w, const double* __restrict__ res,
+                             const double* __restrict__ rho, MonomerSet ms, long ng, double* __restrict__ part) {
+  __shared__ double red[4][32];
+  const int nm = ms.nmon;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ng; i += (long)gridDim.x * blockDim.x) {
+    for (int a = 0; a < nm; ++a) {
+      const double ra = res[(long)a * ng + i], wa = w[(long)a * ng + i], da = rho[(long)a * ng + i];
+      s0 += ra * ra;
+      s1 += wa * wa;
+      s2 += da * wa;
+      for (int b = a + 1; b < nm; ++b) {
+        const double c = ms.chi[a * kMaxMon + b];
+        if (c != 0.0) s3 += c * (da / ms.vol[a]) * (rho[(long)b * ng + i] / ms.vol[b]);
+      }
+    }
+  }
+  s0 = block_sum(s0, red[0]);
+  s1 = block_sum(s1, red[1]);
+  s2 = block_sum(s2, red[2]);
+  s3 = block_sum(s3, red[3]);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x * 4 + 0] = s0;
+    part[blockIdx.x * 4 + 1] = s1;
+    part[blockIdx.x * 4 + 2] = s2;
+    part[blockIdx.x * 4 + 3] = s3;
+  }
+}
+
+void launch_stats(const double* w, const double* res, const double* rho, const MonomerSet& ms, long ng,
+                  double* part, double* out4, cudaStream_t st) {
+  const int nb = red_blocks(ng);
+  stats_kernel<<<nb, 256, 0, st>>>(w, res, rho, ms, ng, part);
+  reduce_parts(part, nb, 4, out4, 1.0, st);
+}
+
+// ------------------------------------------------------------------ Anderson mixing
+__global__ void axpy_kernel(double* __restrict__ y, const double* __restrict__ x, double a, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    y[i] = y[i] + a * x[i];
+}
+
+void launch_axpy(double* y, const double* x, double a, long n, cudaStream_t st) {
+  int nb = (int)((n + 255) / 256);
+  if (nb > 8192) nb = 8192;
+  axpy_kernel<<<nb, 256, 0, st>>>(y, x, a, n);
+}
+
+// Gram sums over all monomer grids (n_all = nmon * Ng): with r = res[ih] and d_m = r - res[ih-m],
+// U[m][n] = sum d_m d_n (m <= n, packed row-major upper triangle) and V[m] = sum d_m r.
+constexpr int kGramTile = 64;
+__global__ void __launch_bounds__(256) gram_kernel(HistPtrs h, int ih, long n, double* __restrict__ part) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* D = reinterpret_cast<double*>(smem_raw);  // [ih][kGramTile]
+  double* R = D + ih * kGramTile;                   // [kGramTile]
+  const int npair = ih * (ih + 1) / 2;
+  const int nout = npair + ih;
+  constexpr int kMaxOwn = 8;
+  double acc[kMaxOwn];
+  int om[kMaxOwn], on[kMaxOwn];
+  for (int j = 0; j < kMaxOwn; ++j) {
+    acc[j] = 0.0;
+    const int o = threadIdx.x + j * blockDim.x;
+    om[j] = -1;
+    on[j] = -1;
+    if (o < npair) {
+      int m = 0, rem = o;
+      while (rem >= ih - m) {
+        rem -= ih - m;
+        ++m;
+      }
+      om[j] = m;
+      on[j] = m + rem;
+    } else if (o < nout) {
+      om[j] = o - npair;
+      on[j] = -2;  // V entry
+    }
+  }
+  const double* r = h.res[ih];
+  for (long t0 = (long)blockIdx.x * kGramTile; t0 < n; t0 += (long)gridDim.x * kGramTile) {
+    for (int idx = threadIdx.x; idx < kGramTile * (ih + 1); idx += blockDim.x) {
+      const int p = idx % kGramTile, m = idx / kGramTile;
+      const long i = t0 + p;
+      const double rv = (i < n) ? r[i] : 0.0;
+      if (m == ih) R[p] = rv;
+      else D[m * kGramTile + p] = (i < n) ? rv - h.res[ih - 1 - m][i] : 0.0;
+    }
+    __syncthreads();
+    for (int j = 0; j < kMaxOwn; ++j) {
+      if (om[j] < 0) continue;
+      const double* a = D + om[j] * kGramTile;
+      const double* b = (on[j] == -2) ? R : D + on[j] * kGramTile;
+      double s = 0.0;
+#pragma unroll 8
+      for (int p = 0; p < kGramTile; ++p) s += a[p] * b[p];
+      acc[j] += s;
+    }
+    __syncthreads();
+  }
+  for (int j = 0; j < kMaxOwn; ++j) {
+    const int o = threadIdx.x + j * blockDim.x;
+    if (o < nout) part[(long)blockIdx.x * nout + o] = acc[j];
+  }
+}
+
+void launch_gram(const HistPtrs& h, int ih, long n_all, double* part, double* out, cudaStream_t st) {
+  const int nout = ih * (ih + 1) / 2 + ih;
+  long nb = (n_all + kGramTile - 1) / kGramTile;
+  if (nb > 2 * 152) nb = 2 * 152;
+  const size_t smem = sizeof(double) * (size_t)(ih + 1) * kGramTile;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  gram_kernel<<<(int)nb, 256, smem, st>>>(h, ih, n_all, part);
+  reduce_parts(part, (int)nb, nout, out, 1.0, st);
+}
+
+// LU with partial pivoting, explicit inverse, Cn = inv(U) V (the inv!(lu!(Umn)) * Vm of
+// anderson.jl:184-189).  status = k+1 when pivot k is exactly zero (LAPACK info > 0).
+__global__ void solve_kernel(const double* __restrict__ packed, int n, double* __restrict__ Cn, int* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ld = n + 1;
+  double* Af = reinterpret_cast<double*>(smem_raw);
+  double* If = Af + n * ld;
+#define A(i, j) Af[(i) * ld + (j)]
+#define Inv(i, j) If[(i) * ld + (j)]
+  __shared__ int perm[kMaxHist];
+  __shared__ int piv;
+  __shared__ int bad;
+  const int npair = n * (n + 1) / 2;
+  const double* V = packed + npair;
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+    const int i = idx / n, j = idx % n;
+    const int m = i < j ? i : j, c = i < j ? j : i;
+    const int o = m * n - m * (m - 1) / 2 + (c - m);
+    A(i, j) = packed[o];
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = i;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      int p = k;
+      double best = fabs(A(k, k));
+      for (int i = k + 1; i < n; ++i) {
+        const double v = fabs(A(i, k));
+        if (v > best) {
+          best = v;
+          p = i;
+        }
+      }
+      piv = p;
+      if (A(p, k) == 0.0 && bad == 0) bad = k + 1;
+    }
+    __syncthreads();
+    if (bad) break;
+    const int p = piv;
+    if (p != k) {
+      for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double t = A(k, j);
+        A(k, j) = A(p, j);
+        A(p, j) = t;
+      }
+      if (threadIdx.x == 0) {
+        const int t = perm[k];
+        perm[k] = perm[p];
+        perm[p] = t;
+      }
+    }
+    __syncthreads();
+    for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A(i, k) /= A(k, k);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < (n - k - 1) * (n - k - 1); idx += blockDim.x) {
+      const int i = k + 1 + idx / (n - k - 1), j = k + 1 + idx % (n - k - 1);
+      A(i, j) -= A(i, k) * A(k, j);
+    }
+    __syncthreads();
+  }
+  if (bad) {
+    if (threadIdx.x == 0) *status = bad;
+    return;
+  }
+  // column col of the inverse: solve L y = P e_col, U x = y
+  for (int col = threadIdx.x; col < n; col += blockDim.x) {
+    double y[kMaxHist];
+    for (int i = 0; i < n; ++i) {
+      double s = (perm[i] == col) ? 1.0 : 0.0;
+      for (int j = 0; j < i; ++j) s -= A(i, j) * y[j];
+      y[i] = s;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double s = y[i];
+      for (int j = i + 1; j < n; ++j) s -= A(i, j) * Inv(j, col);
+      Inv(i, col) = s / A(i, i);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < n; ++j) s += Inv(i, j) * V[j];
+    Cn[i] = s;
+  }
+  if (threadIdx.x == 0) *status = 0;
+#undef A
+#undef Inv
+}
+
+void launch_solve(const double* packed, int ih, double* Cn, int* status, cudaStream_t st) {
+  const size_t smem = 2 * sizeof(double) * (size_t)ih * (ih + 1);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  solve_kernel<<<1, 64, smem, st>>>(packed, ih, Cn, status);
+}
+
+// w = W + lam D,  W = w + sum_nn Cn[nn-1] (f[ih-nn] - f[ih]),  D = r + sum_nn Cn[nn-1] (r[ih-nn] - r)
+__global__ void mix_kernel(double* __restrict__ w, HistPtrs h, int ih, const double* __restrict__ Cn, double lam,
+                           long n) {
+  __shared__ double c[kMaxHist];
+  for (int j = threadIdx.x; j < ih; j += blockDim.x) c[j] = Cn[j];
+  __syncthreads();
+  const double* r = h.res[ih];
+  const double* f = h.field[ih];
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double ri = r[i], fi = f[i];
+    double W = w[i], D = ri;
+    for (int nn = 1; nn <= ih; ++nn) {
+      W += c[nn - 1] * (h.field[ih - nn][i] - fi);
+      D += c[nn - 1] * (h.res[ih - nn][i] - ri);
+    }
+    w[i] = W + lam * D;
+  }
+}
+
+void launch_mix(double* w, const HistPtrs& h, int ih, const double* Cn, double lam, long n_all, cudaStream_t st) {
+  int nb = (int)((n_all + 255) / 256);
+  if (nb > 8192) nb = 8192;
+  mix_kernel<<<nb, 256, 0, st>>>(w, h, ih, Cn, lam, n_all);
+}
+
+}  // namespace pf

@@ -1,0 +1,123 @@
+// Declarations shared by the kernel translation units and the host engine.
+#pragma once
+#include "pf_common.cuh"
+
+namespace pf {
+
+constexpr int kMaxParams = 6;   // triclinic cells have 6 parameters
+constexpr int kMaxMon = 8;      // monomer types per system
+constexpr int kMaxHist = 64;    // Anderson history slots (nhist + 1)
+
+struct GridDims {
+  int nx, ny, nz;
+};
+
+// Reciprocal basis and its parameter derivatives, row-major G[r*3+c] (column c is the
+// reciprocal vector b_c), dGG[(l*3+m)*kMaxParams + p].
+struct CellGeom {
+  int nx, ny, nz, dim;
+  double G[9];
+  double dGG[9 * kMaxParams];
+};
+
+// Operators of one contour step.
+template <typename T>
+struct StepOp {
+  const T* lw;  // exp(-ds vol w / 2), Ng
+  const T* ld;  // exp(-ds b^2 k^2 / 6) / Ng, Nk
+};
+
+// One chain propagation: hist[s] for s = s0, s0+dir, ..., s0+dir*nsteps.
+template <typename T>
+struct ChainJob {
+  T* hist;
+  const StepOp<T>* ops;  // nsteps entries
+  Cx<T>* kbuf;           // 3D grids: half-spectrum scratch of Nk complex
+  int s0, dir, nsteps, pad;
+};
+
+template <typename T>
+struct StressItem {
+  const T* q;
+  const T* qc;
+};
+
+// Block-wide deterministic double sum; the result is valid in thread 0.
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = (l < (int)(blockDim.x >> 5)) ? red[l] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+// ---- propagator launchers (pf_mde_impl.cuh, instantiated in pf_mde_fp32.cu / pf_mde_fp64.cu)
+// Pencils per tile of the z pass (128-byte rows): 16 for float32, 8 for float64.
+template <typename T>
+constexpr int z_tile_pencils() { return sizeof(T) == 4 ? 16 : 8; }
+template <typename T> bool shape_supported(int nx, int ny, int nz);
+template <typename T> void launch_lw(T* lw, const double* w, double coeff, long n, cudaStream_t st);
+template <typename T> void launch_ld(T* ld, const CellGeom& g, double coeff, double scale, long nk, cudaStream_t st);
+void launch_dksq(double* dk, const CellGeom& g, int nparams, long nk, cudaStream_t st);
+template <typename T> void launch_fill(T* a, T v, long n, cudaStream_t st);
+template <typename T>
+void launch_chains(const ChainJob<T>* jobs_dev, int njobs, int maxsteps, const GridDims& d, const Twiddles<T>& tw,
+                   cudaStream_t st);
+// Stress sums: Nz == 1 uses items (device array of nitems); 3D grids use the pointer arrays
+// src_q/src_qc (real grids) and kq/kqc (half-spectrum scratch), each nitems long.
+template <typename T>
+void launch_stress(const StressItem<T>* items, int nitems, const T* const* src_q, const T* const* src_qc,
+                   Cx<T>* const* kq, Cx<T>* const* kqc, const GridDims& d, const double* dksq, int nparams,
+                   double* part, const Twiddles<T>& tw, cudaStream_t st);
+
+// ---- field / density / updater launchers (pf_field.cu)
+struct MonomerSet {
+  int nmon;
+  double vol[kMaxMon];
+  double chi[kMaxMon * kMaxMon];  // symmetric, zero diagonal
+};
+
+// Simpson block description for one species (reference multiblock.jl:182-228).
+struct SimpsonBlocks {
+  int nblocks;
+  int mon[kMaxMon * 2];       // monomer index of each block
+  int bgn[kMaxMon * 2];       // 0-based contour index of the block start
+  int end[kMaxMon * 2];       // 0-based contour index of the block end
+  double ds[kMaxMon * 2];
+};
+
+constexpr int kRedBlocks = 1024;  // partial-sum blocks of the grid reductions
+
+template <typename T>
+void launch_sum(const T* a, long n, double* part, double* out, double div, cudaStream_t st);
+void launch_point_q(const double* w, double vol, long n, double* part, double* Qdev, cudaStream_t st);
+void launch_point_density(double* rho, const double* w, double vol, double phi, const double* Qdev, long n,
+                          cudaStream_t st);
+template <typename T>
+void launch_simpson(double* rho_all, const T* q, const T* qc, bool qc_reversed, int Ns, long ng,
+                    const SimpsonBlocks& blk, double phi, double Nref, const double* Qdev, cudaStream_t st);
+int launch_residuals(double* w, double* pot, double* res, const double* rho, const MonomerSet& ms, long ng,
+                     bool canonical, double* part, double* sums, cudaStream_t st);
+void launch_stats(const double* w, const double* res, const double* rho, const MonomerSet& ms, long ng,
+                  double* part, double* out4, cudaStream_t st);
+void launch_axpy(double* y, const double* x, double a, long n, cudaStream_t st);
+struct HistPtrs {
+  const double* res[kMaxHist];    // logical order 0..ih
+  const double* field[kMaxHist];
+};
+void launch_gram(const HistPtrs& h, int ih, long n_all, double* part, double* out, cudaStream_t st);
+void launch_solve(const double* packed, int ih, double* Cn, int* status, cudaStream_t st);
+void launch_mix(double* w, const HistPtrs& h, int ih, const double* Cn, double lam, long n_all, cudaStream_t st);
+
+}  // namespace pf

@@ -1,0 +1,562 @@
+"""Python mirror of PolyFields.jl's public API, computing on the GB300 through the C ABI.
+
+Names follow the reference's exports (src/PolyFields.jl:29-45) with the Julia ``!`` dropped:
+``add_species!`` is ``add_species``, ``scft!`` is ``scft``, ``fieldinit!`` is ``fieldinit``.
+Objects keep the reference's fields (``Multiblock.Nref``, ``.f_block``, ``.begin_block``,
+``FieldSystem.fields[mid]`` ...), so scripts written against the reference read the same.
+Errors are raised where the reference raises them, with its messages.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import math
+from dataclasses import dataclass, field as dc_field
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+Canonical = "Canonical"
+Grand = "Grand"
+
+FP64 = "fp64"
+FP32 = "fp32"
+_PREC = {FP64: L.PF_FP64, FP32: L.PF_FP32}
+
+
+# =============================================================================
+# Monomers, cells, species, interactions (host descriptors)
+# =============================================================================
+@dataclass(frozen=True)
+class Monomer:
+    """src/system/monomer.jl:7-25."""
+    id: int
+    vol: float = 1.0
+    charge: float = 0.0
+
+
+class UnitCell:
+    """UnitCell(dim, crystal, params...) — src/system/cell.jl:31-54.  The basis matrices are
+    computed by the engine once the cell is attached to a system."""
+
+    def __init__(self, dim: int, crystal: str, *params):
+        if len(params) == 1 and isinstance(params[0], (list, tuple, np.ndarray)):
+            params = tuple(params[0])
+        self.dim = int(dim)
+        self.crystal = str(crystal).lstrip(":")
+        self._params = np.array(params, dtype=np.float64)
+        self._sys = None
+
+    @property
+    def params(self) -> np.ndarray:
+        if self._sys is not None:
+            out = np.zeros(len(self._params))
+            vol = ctypes.c_double()
+            L.check(L.load().pf_get_cell(self._sys._h, L.dptr(out), len(out), ctypes.byref(vol)), self._sys._h)
+            return out
+        return self._params.copy()
+
+    @property
+    def volume(self) -> float:
+        if self._sys is None:
+            raise RuntimeError("the cell volume is computed once the cell belongs to a FieldSystem")
+        vol = ctypes.c_double()
+        L.check(L.load().pf_get_cell(self._sys._h, None, 0, ctypes.byref(vol)), self._sys._h)
+        return vol.value
+
+    @property
+    def nparams(self) -> int:
+        return len(self._params)
+
+
+def chain_grid(N_block: Sequence[float], Ns: int):
+    """src/species/base.jl:27-56."""
+    N = float(sum(N_block))
+    ds = N / Ns
+    begin_block = [1]
+    ds_block = []
+    bgn = 1
+    for nb in N_block:
+        Ns_half = int(math.floor(nb / ds / 2.0 + 0.5))
+        if Ns_half == 0:
+            Ns_half = 1
+            ds_block.append(nb / 2.0)
+        else:
+            ds_block.append(nb / Ns_half / 2.0)
+        bgn += Ns_half * 2
+        begin_block.append(bgn)
+    return N, begin_block, ds_block
+
+
+class Multiblock:
+    """src/species/multiblock.jl:5-60."""
+
+    def __init__(self, mon_block: Sequence[Monomer], N_block: Sequence[int], b_block: Sequence[float],
+                 Ns: int = 100):
+        assert len(mon_block) == len(N_block) == len(b_block)
+        self.monomers = sorted(set(mon_block), key=lambda m: m.id)
+        self.mids = [m.id for m in self.monomers]
+        self.mid_block = [m.id for m in mon_block]
+        self.mid_map: Dict[int, List[int]] = {}
+        for i, mid in enumerate(self.mid_block):
+            self.mid_map.setdefault(mid, []).append(i)
+        self.N = int(sum(N_block))
+        self.N_block = [int(n) for n in N_block]
+        self.Nref_block = [mon_block[i].vol * N_block[i] for i in range(len(mon_block))]
+        self.Nref, self.begin_block, self.ds_block = chain_grid(self.Nref_block, Ns)
+        self.f_block = [v / self.Nref for v in self.Nref_block]
+        self.b_block = [float(b) for b in b_block]
+        self.Ns = self.begin_block[-1] - 1
+        self._sys = None
+        self._isp = -1
+
+    @property
+    def nblocks(self) -> int:
+        return len(self.N_block)
+
+    def hasmonomer(self, mid: int) -> bool:
+        return mid in self.mids
+
+    def monomer_fraction(self, mid: int) -> float:
+        if not self.hasmonomer(mid):
+            return 0.0
+        return sum(self.f_block[i] for i in self.mid_map[mid])
+
+    @property
+    def Q(self) -> float:
+        return self._sys._species_q(self._isp)
+
+    def propagator(self, s: int, conjugate: bool = False) -> np.ndarray:
+        """chain.q[s+1] / chain.qc[s+1] of the reference (s 0-based) from the last density solve."""
+        return self._sys._propagator(self._isp, conjugate, s)
+
+
+def Homopolymer(mon: Monomer, N: int, b: float, Ns: int = 100) -> Multiblock:
+    """multiblock.jl:62-64."""
+    return Multiblock([mon], [N], [b], Ns)
+
+
+def Diblock(amon: Monomer, bmon: Monomer, N: int, f: float, b1: float, b2: float, Ns: int = 100) -> Multiblock:
+    """multiblock.jl:66-72."""
+    N_block = [int(f * N), int((1 - f) * N)]
+    if sum(N_block) != N:
+        raise ValueError(f"Non-integer block lengths for N = {N}, f = {f}.")
+    return Multiblock([amon, bmon], N_block, [b1, b2], Ns)
+
+
+class Point:
+    """src/species/point.jl:9-22."""
+
+    def __init__(self, mon: Monomer):
+        self.mids = [mon.id]
+        self.Nref = mon.vol
+        self._sys = None
+        self._isp = -1
+
+    def hasmonomer(self, mid: int) -> bool:
+        return mid in self.mids
+
+    def monomer_fraction(self, mid: int) -> float:
+        return 1.0 if self.hasmonomer(mid) else 0.0
+
+    @property
+    def Q(self) -> float:
+        return self._sys._species_q(self._isp)
+
+
+class FloryInteraction:
+    """src/interactions/flory.jl:9-49."""
+
+    def __init__(self):
+        self.mids = set()
+        self.chis: Dict[tuple, float] = {}
+
+    def set_interaction(self, alpha, beta, chi: float):
+        alpha = alpha.id if isinstance(alpha, Monomer) else int(alpha)
+        beta = beta.id if isinstance(beta, Monomer) else int(beta)
+        assert alpha != beta
+        pair = (alpha, beta) if alpha <= beta else (beta, alpha)
+        self.mids.update((alpha, beta))
+        self.chis[pair] = float(chi)
+
+
+def set_interaction(itx: FloryInteraction, alpha, beta, chi: float):
+    itx.set_interaction(alpha, beta, chi)
+
+
+# =============================================================================
+# FieldSystem
+# =============================================================================
+class _GridView:
+    """Dict-like view of one family of device grids, keyed by monomer id."""
+
+    def __init__(self, sys: "FieldSystem", kind: int):
+        self._sys, self._kind = sys, kind
+
+    def __getitem__(self, mid: int) -> np.ndarray:
+        out = np.empty(self._sys.shape)
+        L.check(L.load().pf_get_grid(self._sys._h, self._kind, int(mid), L.dptr(out)), self._sys._h)
+        return out
+
+    def __setitem__(self, mid: int, arr) -> None:
+        if self._kind != L.PF_FIELD:
+            raise TypeError("only fields can be assigned")
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        if a.shape != self._sys.shape:
+            raise ValueError(f"Input field dimensions {a.shape} does not match system grid {self._sys.shape}.")
+        L.check(L.load().pf_set_field(self._sys._h, int(mid), L.dptr(a)), self._sys._h)
+
+    def keys(self):
+        return list(self._sys.monomers.keys())
+
+    def __iter__(self):
+        return iter(self.keys())
+
+    def items(self):
+        return [(k, self[k]) for k in self.keys()]
+
+    def values(self):
+        return [self[k] for k in self.keys()]
+
+
+class FieldSystem:
+    """FieldSystem(dims, cell; monomers, ensemble) — src/system/system.jl:51-76.
+
+    ``precision`` selects the propagator arithmetic: "fp64" (the reference's) or "fp32"
+    (densities, residuals, reductions, Anderson and stress sums stay float64)."""
+
+    def __init__(self, dims, cell: UnitCell, monomers: Sequence[Monomer] = (), ensemble: str = Canonical,
+                 precision: str = FP64, mde: str = "RK2"):
+        if ensemble != Canonical:
+            raise ValueError("the GPU engine implements the canonical ensemble")
+        if mde != "RK2":
+            raise ValueError("the GPU engine implements the :RK2 propagator")
+        dims = tuple(int(d) for d in dims)
+        if tuple(sorted(dims, reverse=True)) != dims:
+            raise AssertionError("dims must be given in descending order (src/system/system.jl:58)")
+        lib = L.load()
+        h = ctypes.c_void_p()
+        st = lib.pf_system_create(ctypes.byref(h), dims[0], dims[1], dims[2], _PREC[precision])
+        if st != L.PF_OK:
+            raise L.PolyFieldsError(st, f"pf_system_create{dims}: {lib.pf_status_string(st).decode()}")
+        self._h = h
+        self.dims = dims
+        self.shape = (dims[2], dims[1], dims[0])
+        self.ensemble = ensemble
+        self.monomers: Dict[int, Monomer] = {}
+        self.species: list = []
+        self.phi_species: List[float] = []
+        self.interactions: list = []
+        self.cell = None
+        self.add_cell(cell)
+        for m in monomers:
+            self.add_monomer(m)
+        self.fields = _GridView(self, L.PF_FIELD)
+        self.density = _GridView(self, L.PF_DENSITY)
+        self.residuals = _GridView(self, L.PF_RESIDUAL)
+        self.potentials = _GridView(self, L.PF_POTENTIAL)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                L.load().pf_system_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # -- composition
+    @property
+    def ngrid(self) -> int:
+        return self.dims[0] * self.dims[1] * self.dims[2]
+
+    @property
+    def precision(self) -> str:
+        p = ctypes.c_int()
+        L.check(L.load().pf_get_precision(self._h, ctypes.byref(p)), self._h)
+        return FP64 if p.value == L.PF_FP64 else FP32
+
+    @precision.setter
+    def precision(self, value: str) -> None:
+        L.check(L.load().pf_set_precision(self._h, _PREC[value]), self._h)
+
+    def add_cell(self, cell: UnitCell) -> None:
+        p = np.ascontiguousarray(cell._params, dtype=np.float64)
+        L.check(L.load().pf_set_cell(self._h, cell.dim, cell.crystal.encode(), L.dptr(p), len(p)), self._h)
+        cell._sys = self
+        self.cell = cell
+
+    def add_monomer(self, mon: Monomer) -> None:
+        L.check(L.load().pf_add_monomer(self._h, mon.id, mon.vol, mon.charge), self._h)
+        self.monomers[mon.id] = mon
+
+    def add_species(self, species, val: float) -> None:
+        lib = L.load()
+        if isinstance(species, Multiblock):
+            mids = np.array(species.mid_block, dtype=np.int32)
+            Nb = np.array(species.N_block, dtype=np.int32)
+            bb = np.array(species.b_block, dtype=np.float64)
+            for mid in species.mid_block:
+                if mid in self.monomers and self.monomers[mid] not in species.monomers:
+                    raise ValueError(f"monomer {mid} of the species differs from the system's")
+            L.check(lib.pf_add_multiblock(self._h, len(mids), L.iptr(mids), L.iptr(Nb), L.dptr(bb),
+                                          species.Ns, float(val)), self._h)
+        elif isinstance(species, Point):
+            L.check(lib.pf_add_point(self._h, species.mids[0], float(val)), self._h)
+        else:
+            raise TypeError(f"unsupported species {type(species).__name__}")
+        species._sys = self
+        species._isp = len(self.species)
+        self.species.append(species)
+        self.phi_species.append(float(val))
+
+    def add_interaction(self, itx: FloryInteraction) -> None:
+        if not isinstance(itx, FloryInteraction):
+            raise TypeError("the GPU engine implements FloryInteraction")
+        for (a, b), chi in itx.chis.items():
+            L.check(L.load().pf_set_flory(self._h, a, b, chi), self._h)
+        self.interactions.append(itx)
+
+    # -- hot path (system.jl)
+    def validate(self) -> None:
+        L.check(L.load().pf_validate(self._h), self._h)
+
+    def density_update(self) -> None:
+        L.check(L.load().pf_density(self._h), self._h)
+
+    def residuals_update(self) -> None:
+        L.check(L.load().pf_residuals(self._h), self._h)
+
+    def free_energy(self) -> float:
+        v = ctypes.c_double()
+        L.check(L.load().pf_free_energy(self._h, ctypes.byref(v)), self._h)
+        return v.value
+
+    def free_energy_bulk(self) -> float:
+        v = ctypes.c_double()
+        L.check(L.load().pf_free_energy_bulk(self._h, ctypes.byref(v)), self._h)
+        return v.value
+
+    def field_error(self) -> float:
+        v = ctypes.c_double()
+        L.check(L.load().pf_field_error(self._h, ctypes.byref(v)), self._h)
+        return v.value
+
+    def scfstress(self) -> np.ndarray:
+        out = np.zeros(self.cell.nparams)
+        L.check(L.load().pf_scfstress(self._h, L.dptr(out), len(out)), self._h)
+        return out
+
+    def _species_q(self, isp: int) -> float:
+        v = ctypes.c_double()
+        L.check(L.load().pf_species_q(self._h, isp, ctypes.byref(v)), self._h)
+        return v.value
+
+    def _propagator(self, isp: int, conjugate: bool, s: int) -> np.ndarray:
+        out = np.empty(self.shape)
+        L.check(L.load().pf_get_propagator(self._h, isp, 1 if conjugate else 0, s, L.dptr(out)), self._h)
+        return out
+
+    def set_timing(self, enable: bool) -> None:
+        L.check(L.load().pf_set_timing(self._h, 1 if enable else 0), self._h)
+
+    def last_timing(self):
+        a, b, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        L.check(L.load().pf_last_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)), self._h)
+        return a.value, b.value, n.value
+
+    def synchronize(self) -> None:
+        L.check(L.load().pf_synchronize(self._h), self._h)
+
+
+def add_species(sys: FieldSystem, species, val: float) -> None:
+    sys.add_species(species, val)
+
+
+def add_interaction(sys: FieldSystem, itx) -> None:
+    sys.add_interaction(itx)
+
+
+def validate(sys: FieldSystem) -> None:
+    sys.validate()
+
+
+def density(sys: FieldSystem) -> None:
+    """density!(sys)."""
+    sys.density_update()
+
+
+def residuals(sys: FieldSystem) -> None:
+    """residuals!(sys)."""
+    sys.residuals_update()
+
+
+def free_energy(sys: FieldSystem) -> float:
+    return sys.free_energy()
+
+
+def free_energy_bulk(sys: FieldSystem) -> float:
+    return sys.free_energy_bulk()
+
+
+def field_error(sys: FieldSystem) -> float:
+    return sys.field_error()
+
+
+def scfstress(sys: FieldSystem) -> np.ndarray:
+    return sys.scfstress()
+
+
+# =============================================================================
+# Updaters and driver
+# =============================================================================
+class AndersonUpdater:
+    """AndersonUpdater(; nhist = 50, iter_euler = 1, lam_euler = 0.01) — anderson.jl:36-47.
+    The history lives on the device of the system it is set up with."""
+
+    def __init__(self, nhist: int = 50, iter_euler: int = 1, lam_euler: float = 0.01):
+        self.nhist = int(nhist)
+        self.iter_euler = max(1, int(iter_euler))
+        self.lam_euler = float(lam_euler)
+        self.system: Optional[FieldSystem] = None
+
+    def _bind(self, sys: FieldSystem) -> None:
+        if self.system is not sys:
+            L.check(L.load().pf_anderson_create(sys._h, self.nhist, self.iter_euler, self.lam_euler), sys._h)
+            self.system = sys
+
+    def setup(self, sys: FieldSystem) -> None:
+        """setup!(updater, sys) — anderson.jl:54-92."""
+        self._bind(sys)
+        L.check(L.load().pf_anderson_setup(sys._h), sys._h)
+
+    def step(self) -> None:
+        """step!(updater) — anderson.jl:98-228."""
+        if self.system is None:
+            raise RuntimeError("AndersonUpdater is not set up")
+        L.check(L.load().pf_anderson_step(self.system._h), self.system._h)
+
+
+class DomainUpdater:
+    """DomainUpdater(; nper = 10, nskip = 200, lam = 0.1, pmax = 1.0, rlxn = 0.5) — domain.jl:20-24."""
+
+    def __init__(self, nper: int = 10, nskip: int = 200, lam: float = 0.1, pmax: float = 1.0, rlxn: float = 0.5):
+        self.nper, self.nskip = int(nper), int(nskip)
+        self.lam, self.pmax, self.rlxn = float(lam), float(pmax), float(rlxn)
+        self.system: Optional[FieldSystem] = None
+
+    def _bind(self, sys: FieldSystem) -> None:
+        L.check(L.load().pf_domain_create(sys._h, self.nper, self.nskip, self.lam, self.pmax, self.rlxn), sys._h)
+        self.system = sys
+
+    def setup(self, sys: FieldSystem) -> None:
+        self._bind(sys)
+        L.check(L.load().pf_domain_setup(sys._h), sys._h)
+
+    def step(self, nsteps: int = 1, tol: float = 1e-5) -> None:
+        L.check(L.load().pf_domain_step(self.system._h, int(nsteps)), self.system._h)
+
+    def stress_error(self) -> float:
+        v = ctypes.c_double()
+        L.check(L.load().pf_domain_stress_error(self.system._h, ctypes.byref(v)), self.system._h)
+        return v.value
+
+
+def updater_with_system(cls, sys: FieldSystem, **kwargs):
+    """src/updaters/base.jl:16-20."""
+    u = cls(**kwargs)
+    u.setup(sys)
+    return u
+
+
+def setup(updater, sys: FieldSystem) -> None:
+    updater.setup(sys)
+
+
+def step(updater, **kwargs) -> None:
+    updater.step(**kwargs)
+
+
+@dataclass
+class SCFTOptions:
+    """src/simulate.jl:12-19, plus ``mixed_switch_ferr``: with an fp32 system, iterate in fp32
+    until ferr < mixed_switch_ferr, then continue in fp64 (0 disables the switch)."""
+    nsteps: int = 100
+    nsout: int = 0
+    nsave: int = 0
+    ftol: float = 1e-5
+    stol: float = 1e-4
+    savepath: str = ""
+    mixed_switch_ferr: float = 0.0
+
+
+@dataclass
+class SCFTResults:
+    """src/simulate.jl:26-33 (+ the step at which the precision switched, -1 if never)."""
+    time: float
+    nsteps: int
+    converged: bool
+    ferr: float
+    serr: float
+    fhelm: float
+    switch_step: int = -1
+
+
+def scft(sys: FieldSystem, updater: AndersonUpdater, domain: Optional[DomainUpdater] = None,
+         opts: Optional[SCFTOptions] = None) -> SCFTResults:
+    """scft!(sys, updater; domain, opts) — src/simulate.jl:60-148."""
+    if not isinstance(updater, AndersonUpdater):
+        raise TypeError("the GPU engine implements scft! with the AndersonUpdater")
+    opts = opts or SCFTOptions()
+    updater._bind(sys)
+    if domain is not None:
+        domain._bind(sys)
+    o = L.ScftOptions(opts.nsteps, opts.nsout, opts.nsave, 0, opts.ftol, opts.stol, opts.mixed_switch_ferr)
+    r = L.ScftResults()
+    L.check(L.load().pf_scft(sys._h, ctypes.byref(o), 1 if domain is not None else 0, ctypes.byref(r)), sys._h)
+    if opts.savepath:
+        savefields(sys, opts.savepath)
+    return SCFTResults(r.time, r.nsteps, bool(r.converged), r.ferr, r.serr, r.fhelm, r.switch_step)
+
+
+# =============================================================================
+# Field initialisation and IO (src/fileio.jl)
+# =============================================================================
+def fieldinit(sys: FieldSystem, fields: Optional[Dict[int, np.ndarray]] = None, *, seed: int = -1,
+              scale: float = 0.1) -> None:
+    """fieldinit!(sys, fields::Dict) (fileio.jl:25-54) or, without ``fields``,
+    fieldinit!(sys; seed, scale) (fileio.jl:14-23) with NumPy's PCG64 normal stream in place
+    of Julia's MersenneTwister randn."""
+    if fields is None:
+        rng = np.random.Generator(np.random.PCG64(seed if seed >= 0 else None))
+        fields = {mid: scale * rng.standard_normal(sys.shape) for mid in sorted(sys.monomers)}
+    for mid, arr in fields.items():
+        if mid in sys.monomers:
+            sys.fields[mid] = arr
+    sys.residuals_update()
+
+
+def loadfields(path: str) -> dict:
+    """loadfields (fileio.jl:99-132): nested [z][y][x] JSON lists -> arrays of shape (Nz, Ny, Nx)."""
+    with open(path) as fh:
+        raw = json.load(fh)
+    grid = tuple(int(g) for g in raw["grid"])
+    mids = [int(m) for m in raw["mids"]]
+    fields = {m: np.array(raw["fields"][str(m)], dtype=np.float64).reshape(grid[2], grid[1], grid[0]) for m in mids}
+    return {"dim": int(raw["dim"]), "grid": grid, "mids": mids, "crystal": raw["crystal"],
+            "cell_params": [float(p) for p in raw["cell_params"]], "field_type": raw["field_type"],
+            "fields": fields}
+
+
+def savefields(sys: FieldSystem, path: str, field_type: str = "omega") -> None:
+    """savefields (fileio.jl:77-97): the same JSON layout the reference writes."""
+    import datetime
+    grids = sys.density if field_type == "rho" else sys.fields
+    d = {"dim": sum(1 for n in sys.dims if n > 1), "grid": list(sys.dims), "mids": sorted(sys.monomers),
+         "date": datetime.datetime.now().strftime("%Y-%m-%d %H:%M:%S"), "crystal": sys.cell.crystal,
+         "cell_params": [float(p) for p in sys.cell.params], "field_type": field_type,
+         "fields": {str(m): grids[m].tolist() for m in sorted(sys.monomers)}}
+    with open(path, "w") as fh:
+        json.dump(d, fh, indent=4)

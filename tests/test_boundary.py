@@ -1,0 +1,80 @@
+"""CPU checks of the drop-in boundary: the C-ABI library exports every declared entry point
+and the Python mirror's host-side logic matches the reference (no GPU calls)."""
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+import pf_oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "polyfields_gpu.h")
+LIB = os.path.join(ROOT, "polyfields.jl_gb300", "polyfields", "libpolyfields_gpu.so")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pf_[a-z_0-9]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    if not os.path.exists(LIB):
+        subprocess.run([sys.executable, os.path.join(ROOT, "polyfields.jl_gb300", "build.py")], check=True)
+    return LIB
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for n in ("pf_system_create", "pf_scft", "pf_anderson_step", "pf_domain_step", "pf_scfstress", "pf_propagate"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(lib_path):
+    out = subprocess.run(["nm", "-D", "--defined-only", lib_path], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\sT\s(pf_[a-z_0-9]+)", out))
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+
+
+def test_library_loads_and_binds_every_symbol(lib_path):
+    import polyfields._lib as L
+    lib = L.load(lib_path)
+    assert lib.pf_version() == 100
+    assert set(L.SIGNATURES) == set(declared_functions())
+    assert lib.pf_status_string(L.PF_ENAN).decode() == "Diverging field updater -- breaking."
+
+
+def test_python_mirror_chain_grid_matches_oracle():
+    import polyfields as pf
+    for Nb, Ns in (([50, 50], 100), ([35, 65], 100), ([40, 60], 200), ([50], 200), ([10] * 6, 60), ([3, 97], 100)):
+        assert pf.chain_grid(Nb, Ns) == O.chain_grid(Nb, Ns)
+    a, b = pf.Monomer(1, 2.0), pf.Monomer(2)
+    ch = pf.Diblock(a, b, 100, 0.25, 1.0, 1.0, 200)
+    oc = O.Diblock(O.Monomer(1, 2.0), O.Monomer(2), 100, 0.25, 1.0, 1.0, 200)
+    assert ch.f_block == oc.f_block and ch.Nref_block == oc.Nref_block and ch.Ns == oc.Ns
+    with pytest.raises(ValueError):
+        pf.Diblock(a, b, 100, 0.29, 1.0, 1.0, 100)
+
+
+def test_python_mirror_rejects_unsorted_dims():
+    import polyfields as pf
+    with pytest.raises(AssertionError):
+        pf.FieldSystem((1, 64, 1), pf.UnitCell(1, "lamellar", 10.0))
+
+
+def test_no_gpu_fails_loudly(lib_path):
+    """Without a CUDA device the engine raises instead of falling back to the CPU."""
+    import polyfields as pf
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    with pytest.raises(pf.PolyFieldsError):
+        pf.FieldSystem((64, 1, 1), pf.UnitCell(1, "lamellar", 10.0))
