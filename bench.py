@@ -1,0 +1,300 @@
+#!/usr/bin/env python
+"""Benchmark: SCFT iterations/s of the large blend at 128^3 on one GB300.
+
+Workload (one "step" = one scft! iteration = AndersonUpdater.step!): AB diblock N100 fA0.4
+(phi 0.8) + A homopolymer N50 (phi 0.2), chi 0.2, Ns 200, 128^3 grid, cubic cell L0 14,
+double-gyroid start + 0.05 seeded noise, Anderson nhist 20.  One iteration is one density
+solve -- 600 MDE contour steps (diblock forward + backward, homopolymer forward), Simpson
+integration, residuals -- and the Anderson Gram/solve/mix.  The timed region runs the FP32
+propagators of the mixed-precision path (densities, residuals, Gram and solve in FP64); the
+FP64 propagator rate is measured after it on the same state.
+
+  python bench.py [--steps K] [--warmup W]            # GPU engine (one JSON line)
+  python bench.py --impl reference [--steps K ...]    # the FP64 CPU restatement (oracle)
+
+Inputs are synthetic (seeded NumPy PCG64 fields of the benchmark's shapes) and the working
+set (propagator histories, ~5 GB) is far larger than the 129 MB L2.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "polyfields.jl_gb300"))
+
+N_GRID = 128
+MDE_STEPS_PER_ITER = 600  # 200 (diblock q) + 200 (diblock qc) + 200 (homopolymer q)
+METRIC = "SCFT iters/s at 128^3 (mixed path: FP32 propagators, FP64 reductions/Anderson)"
+UNIT = "iters/s"
+WORKLOAD = {
+    "workload": "large blend 128^3: AB diblock N100 fA0.4 phi0.8 + A homopolymer N50 phi0.2, chi0.2, Ns200, "
+                "cubic L0=14, double-gyroid init, Anderson nhist20",
+    "grid": [N_GRID, N_GRID, N_GRID],
+    "mde_steps_per_iter": MDE_STEPS_PER_ITER,
+    "l2_policy": "inputs larger than L2 (propagator histories ~5 GB per iteration)",
+}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax = float(parts[2])
+                except ValueError:
+                    continue
+                for name, flag in zip(names, parts[5:9]):
+                    if flag.lower().startswith("active"):
+                        reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline_sample(nsteps=80):
+    """The FP64 CPU restatement (oracle, NumPy + pocketfft on all cores) on a bounded sample of
+    the same workload: nsteps contour steps of the 128^3 propagator, scaled to one SCFT
+    iteration (600 contour steps).  The Simpson integration and the Anderson update are not in
+    the sample, so the CPU rate is an upper bound."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import pf_oracle as O
+    O.FFT_WORKERS = -1
+    dims = (N_GRID,) * 3
+    cell = O.UnitCell(3, "cubic", 14.0)
+    cell.setup(dims)
+    solver = O.PseudoSpectralSolver(dims)
+    rng = np.random.Generator(np.random.PCG64(12345))
+    w = 0.05 * rng.standard_normal(solver.shape)
+    solver.update(w, cell.ksq, 1.0, 1.0, 0.5)
+    q = np.ones(solver.shape)
+    out = np.empty_like(q)
+    solver.propagate(q, out)
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        solver.propagate(q, out)
+        q, out = out, q
+    dt = time.perf_counter() - t0
+    return {"value": (nsteps / dt) / MDE_STEPS_PER_ITER, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{nsteps} contour steps of the 128^3 FP64 propagator (NumPy/pocketfft, FFTs on all cores, "
+                      f"elementwise single-threaded) in {dt:.1f} s, scaled to 600 steps per iteration",
+            "mde_steps_per_s": nsteps / dt}
+
+
+def run_reference(args):
+    """Reference arm: the FP64 CPU restatement of the reference's path (the oracle); each step
+    is a bounded sample (20 contour steps of the 128^3 propagator) scaled to iterations/s."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import pf_oracle as O
+    O.FFT_WORKERS = -1
+    dims = (N_GRID,) * 3
+    cell = O.UnitCell(3, "cubic", 14.0)
+    cell.setup(dims)
+    solver = O.PseudoSpectralSolver(dims)
+    rng = np.random.Generator(np.random.PCG64(12345))
+    solver.update(0.05 * rng.standard_normal(solver.shape), cell.ksq, 1.0, 1.0, 0.5)
+    q = np.ones(solver.shape)
+    out = np.empty_like(q)
+    per_step = 20
+
+    def one():
+        nonlocal q, out
+        for _ in range(per_step):
+            solver.propagate(q, out)
+            q, out = out, q
+
+    for _ in range(args.warmup):
+        one()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one()
+    dt = time.perf_counter() - t0
+    steps_per_s = per_step * args.steps / dt
+    value = steps_per_s / MDE_STEPS_PER_ITER
+    sample = (f"{per_step} contour steps of the 128^3 FP64 propagator per step (NumPy/pocketfft, FFTs on all cores), "
+              f"scaled to 600 contour steps per SCFT iteration; Simpson and Anderson work not included")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": WORKLOAD, "mde_steps_per_s": steps_per_s,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import polyfields as pf
+    from polyfields import _lib as L
+    from polyfields.workloads import blend3d_system
+
+    lib = L.load()
+    if args.gpus != 1:
+        raise SystemExit("the engine runs one SCFT instance per GPU; run with --gpus 1")
+    n = args.size
+    sysm = blend3d_system(pf, n=n, precision="fp32")
+    ng = n ** 3
+    upd = pf.AndersonUpdater(nhist=20)
+    upd.setup(sysm)
+    sysm.set_timing(True)
+    for _ in range(args.warmup):
+        upd.step()
+    sysm.synchronize()
+
+    # ---- timed region: K scft! iterations with FP32 propagators
+    clocks = ClockSampler()
+    clocks.start()
+    l0 = lib.pf_launch_count()
+    prop_ms = 0.0
+    dens_ms = 0.0
+    L.check(lib.pf_record_event(sysm._h, 0), sysm._h)
+    t_host = time.perf_counter()
+    for _ in range(args.steps):
+        upd.step()
+        a, b, nmde = sysm.last_timing()
+        prop_ms += a
+        dens_ms += b
+    L.check(lib.pf_record_event(sysm._h, 1), sysm._h)
+    import ctypes
+    ms = ctypes.c_double()
+    L.check(lib.pf_elapsed_ms(sysm._h, 0, 1, ctypes.byref(ms)), sysm._h)
+    t_host = time.perf_counter() - t_host
+    launches = lib.pf_launch_count() - l0
+    clk = clocks.stop()
+    ms_per_step = ms.value / args.steps
+    value = 1000.0 / ms_per_step
+    prop_step_ms = prop_ms / args.steps
+    mde_step_us = 1000.0 * prop_step_ms / nmde
+    ferr = sysm.field_error()
+    fhelm = sysm.free_energy()
+
+    # ---- roofline of the dominant kernel pair (one MDE contour step: xy_step + z_step)
+    peak, peak_kind = measured_peaks()
+    alg_bytes = 3 * 4 * ng  # read q_s (f32), read LW (f32), write q_{s+1} (f32)
+    achieved = alg_bytes / (mde_step_us * 1e-6) / 1e9
+    roofline = {"bound": "hbm", "kernel": "MDE contour step (xy_step_kernel<float,128,128> + z_step_kernel<float,128>)",
+                "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_launch": alg_bytes,
+                "avg_step_us": mde_step_us}
+
+    # ---- e2e through the public API with host buffers (pinned when torch is present)
+    try:
+        import torch
+        host = {m: torch.empty((n, n, n), dtype=torch.float64, pin_memory=True).numpy() for m in (1, 2)}
+    except Exception:
+        host = {m: np.empty((n, n, n)) for m in (1, 2)}
+    for m in (1, 2):
+        host[m][...] = sysm.fields[m]
+    e2e_steps = max(1, min(args.steps, 5))
+    sysm.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for m in (1, 2):
+            L.check(lib.pf_set_field(sysm._h, m, L.dptr(host[m])), sysm._h)
+        upd.step()
+        for m in (1, 2):
+            L.check(lib.pf_get_grid(sysm._h, L.PF_FIELD, m, L.dptr(host[m])), sysm._h)
+        _ = sysm.free_energy()
+    e2e_dt = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": 1.0 / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * ng, "d2h_bytes_per_step": 2 * 8 * ng + 8,
+           "api": "pf_set_field x2 + pf_anderson_step + pf_get_grid x2 + pf_free_energy"}
+
+    # ---- FP64 propagators on the same state (the plain FP64 GPU solver's iteration rate)
+    fp64 = None
+    if args.fp64_steps > 0:
+        sysm.precision = "fp64"
+        upd.step()
+        L.check(lib.pf_record_event(sysm._h, 2), sysm._h)
+        for _ in range(args.fp64_steps):
+            upd.step()
+        L.check(lib.pf_record_event(sysm._h, 3), sysm._h)
+        m64 = ctypes.c_double()
+        L.check(lib.pf_elapsed_ms(sysm._h, 2, 3, ctypes.byref(m64)), sysm._h)
+        a64, _, _ = sysm.last_timing()
+        fp64 = {"iters_per_s": 1000.0 * args.fp64_steps / m64.value, "ms_per_iter": m64.value / args.fp64_steps,
+                "mde_step_us": 1000.0 * a64 / nmde}
+
+    cpu = cpu_baseline_sample(args.cpu_steps) if args.cpu_steps > 0 else None
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 propagators + f64 reductions", "data": "synthetic", "config": dict(WORKLOAD, size=n),
+            "mde_steps_per_s": value * nmde, "mde_steps_per_iter": nmde, "propagate_ms_per_iter": prop_step_ms,
+            "density_ms_per_iter": dens_ms / args.steps, "host_ms_per_step": 1000.0 * t_host / args.steps,
+            "fp64": fp64, "mixed_vs_fp64_iter_speedup": (value / fp64["iters_per_s"]) if fp64 else None,
+            "ferr": ferr, "fhelm": fhelm, "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clk, "cpu_baseline": cpu}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=N_GRID, help="grid points per axis (default 128)")
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=80, help="contour steps of the CPU baseline sample (0: skip)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -155,6 +155,12 @@ int pf_propagate(pf_system* sys, const double* omega, double vol, double b, doub
  * events on the handle's stream; 0 if not recorded.  Enable with pf_set_timing(sys, 1). */
 int pf_set_timing(pf_system* sys, int enable);
 int pf_last_timing(const pf_system* sys, double* propagate_ms, double* density_ms, int* mde_steps);
+/* Record CUDA event slot (0..7) on the handle's stream; elapsed device time between two
+ * recorded slots (waits for slot b). */
+int pf_record_event(pf_system* sys, int slot);
+int pf_elapsed_ms(pf_system* sys, int a, int b, double* ms);
+/* Kernels launched by this library so far (all handles). */
+long pf_launch_count(void);
 /* Synchronise the handle's stream. */
 int pf_synchronize(pf_system* sys);
 

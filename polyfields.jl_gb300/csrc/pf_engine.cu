@@ -329,6 +329,9 @@ struct Species {
   std::vector<std::unique_ptr<DevBuf>> lw[2], ld[2];
   DevBuf ops[2];  // StepOp<T> of the forward then backward job
   DevBuf kbuf[2][2];
+  // float32 histories are rescaled per contour step (ChainJob::csc/lsc): factors of the
+  // forward and backward jobs, the Simpson factors fac[s] and the mean of the last q
+  DevBuf csc[2], lsc[2], fac, meanq;
   int ld_version[2] = {-1, -1};
   DevBuf Qdev;
   bool Q_valid = false;
@@ -394,6 +397,7 @@ struct System {
   bool jobs_dirty[2] = {true, true};
   bool timing = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t uev[8] = {};  // user events (pf_record_event)
   double t_prop_ms = 0.0, t_dens_ms = 0.0;
   int mde_steps = 0;
 
@@ -436,10 +440,13 @@ struct System {
     build_twiddles<double>(0);
     build_twiddles<float>(1);
     for (auto& e : ev) PF_CU(cudaEventCreate(&e));
+    for (auto& e : uev) PF_CU(cudaEventCreate(&e));
   }
   ~System() {
     if (st) cudaStreamSynchronize(st);
     for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    for (auto& e : uev)
       if (e) cudaEventDestroy(e);
     if (st) cudaStreamDestroy(st);
   }
@@ -599,6 +606,9 @@ struct System {
     if (species.empty()) throw PFError(E_STATE, "no species added");
   }
 
+  // float32 propagators are rescaled per contour step; float64 ones follow the reference as is
+  static bool scaled(int p) { return p == 1; }
+
   // ---------------------------------------------------------------- propagator setup
   template <typename T>
   void ensure_prop(int p) {
@@ -644,8 +654,26 @@ struct System {
           kb1 = sp.kbuf[p][1].as<Cx<T>>();
         }
       }
-      hjobs.push_back(ChainJob<T>{sp.q[p].as<T>(), ops, kb0, 0, +1, sp.Ns, 0});
-      if (nb > 1) hjobs.push_back(ChainJob<T>{sp.qc[p].as<T>(), ops + sp.Ns, kb1, sp.Ns, -1, sp.Ns, 0});
+      float* c0 = nullptr;
+      float* c1 = nullptr;
+      double* l0 = nullptr;
+      double* l1 = nullptr;
+      if (scaled(p)) {
+        for (int j = 0; j < 2; ++j) {
+          sp.csc[j].alloc(sizeof(float) * sp.Ns);
+          sp.lsc[j].alloc(sizeof(double) * sp.Ns);
+        }
+        sp.fac.alloc(sizeof(double) * (sp.Ns + 1));
+        sp.meanq.alloc(sizeof(double));
+        c0 = sp.csc[0].as<float>();
+        l0 = sp.lsc[0].as<double>();
+        if (nb > 1) {
+          c1 = sp.csc[1].as<float>();
+          l1 = sp.lsc[1].as<double>();
+        }
+      }
+      hjobs.push_back(ChainJob<T>{sp.q[p].as<T>(), ops, kb0, c0, l0, 0, +1, sp.Ns, 0});
+      if (nb > 1) hjobs.push_back(ChainJob<T>{sp.qc[p].as<T>(), ops + sp.Ns, kb1, c1, l1, sp.Ns, -1, sp.Ns, 0});
       maxsteps = std::max(maxsteps, sp.Ns);
     }
     njobs = (int)hjobs.size();
@@ -686,7 +714,17 @@ struct System {
     for (auto& spp : species) {
       Species& sp = *spp;
       if (sp.kind == 0) {
-        launch_sum<T>(sp.q[p].as<T>() + (long)sp.Ns * ng, ng, part.as<double>(), sp.Qdev.as<double>(), (double)ng, st);
+        const double* fac = nullptr;
+        if (scaled(p)) {
+          launch_sum<T>(sp.q[p].as<T>() + (long)sp.Ns * ng, ng, part.as<double>(), sp.meanq.as<double>(), (double)ng,
+                        st);
+          launch_scale_finalize(sp.lsc[0].as<double>(), sp.lsc[1].as<double>(), sp.nblocks() == 1, sp.Ns,
+                                sp.meanq.as<double>(), sp.Qdev.as<double>(), sp.fac.as<double>(), st);
+          fac = sp.fac.as<double>();
+        } else {
+          launch_sum<T>(sp.q[p].as<T>() + (long)sp.Ns * ng, ng, part.as<double>(), sp.Qdev.as<double>(), (double)ng,
+                        st);
+        }
         SimpsonBlocks sb{};
         sb.nblocks = sp.nblocks();
         for (int b = 0; b < sb.nblocks; ++b) {
@@ -697,7 +735,7 @@ struct System {
         }
         const T* qc = sp.nblocks() > 1 ? sp.qc[p].as<T>() : nullptr;
         launch_simpson<T>(rho.as<double>(), sp.q[p].as<T>(), qc, sp.nblocks() == 1, sp.Ns, ng, sb, sp.phi, sp.Nref,
-                          sp.Qdev.as<double>(), st);
+                          sp.Qdev.as<double>(), fac, st);
       } else {
         const int mid = sp.mids[0];
         const double vol = monomers.at(mid).first;
@@ -827,6 +865,17 @@ struct System {
     }
     const int nit = (int)items.size();
     std::vector<double> qint(nit * (size_t)npr, 0.0);
+    // rescaled histories: each term carries fac[s] = exp(-L_s - L'_s - log Q), so Q is
+    // already divided out
+    std::vector<double> hfac;
+    std::vector<int> item_s;
+    if (scaled(p)) {
+      hfac.resize(sp.Ns + 1);
+      PF_CU(cudaMemcpyAsync(hfac.data(), sp.fac.p, sizeof(double) * (sp.Ns + 1), cudaMemcpyDeviceToHost, st));
+      PF_CU(cudaStreamSynchronize(st));
+      for (int b = 0; b < sp.nblocks(); ++b)
+        for (int s = sp.begin_block[b]; s <= sp.begin_block[b + 1]; ++s) item_s.push_back(s - 1);
+    }
     const GridDims d{nx, ny, nz};
     if (nz == 1) {
       std::vector<StressItem<T>> h(nit);
@@ -877,12 +926,14 @@ struct System {
       }
     }
     const double ng2 = (double)ng * (double)ng;
-    for (int i = 0; i < nit; ++i)
+    for (int i = 0; i < nit; ++i) {
+      const double f = scaled(p) ? hfac[item_s[i]] : 1.0;
       for (int k = 0; k < npr; ++k)
-        dQ[k] -= items[i].b * items[i].b * items[i].w * qint[(size_t)i * npr + k] / 6.0 / ng2;
+        dQ[k] -= items[i].b * items[i].b * items[i].w * (qint[(size_t)i * npr + k] * f) / 6.0 / ng2;
+    }
     for (int k = 0; k < npr; ++k) {
       dQ[k] /= 3.0;
-      dQ[k] /= sp.Q * sp.Nref;
+      dQ[k] /= scaled(p) ? sp.Nref : sp.Q * sp.Nref;
     }
     return dQ;
   }
@@ -1143,7 +1194,7 @@ struct System {
       kb.alloc(sizeof(Cx<T>) * nk);
       kp = kb.as<Cx<T>>();
     }
-    ChainJob<T> hj{hist.as<T>(), ops.as<StepOp<T>>(), kp, 0, +1, nsteps, 0};
+    ChainJob<T> hj{hist.as<T>(), ops.as<StepOp<T>>(), kp, nullptr, nullptr, 0, +1, nsteps, 0};
     job.alloc(sizeof(hj));
     PF_CU(cudaMemcpyAsync(job.p, &hj, sizeof(hj), cudaMemcpyHostToDevice, st));
     launch_chains<T>(job.as<ChainJob<T>>(), 1, nsteps, GridDims{nx, ny, nz}, tw<T>(p), st);
@@ -1344,8 +1395,17 @@ int pf_get_propagator(pf_system* sys, int isp, int conjugate, int s_idx, double*
     } else {
       std::vector<float> t(s.ng);
       PF_CU(cudaMemcpyAsync(t.data(), src->as<float>() + off, sizeof(float) * s.ng, cudaMemcpyDeviceToHost, s.st));
+      // undo the per-step rescaling: stored = true * exp(L), L the sum of the applied logs
+      const int job = (conjugate && sp.nblocks() > 1) ? 1 : 0;
+      const int idx = (int)(off / s.ng);
+      const int nlog = job == 0 ? idx : sp.Ns - idx;
+      std::vector<double> l(sp.Ns);
+      PF_CU(cudaMemcpyAsync(l.data(), sp.lsc[job].p, sizeof(double) * sp.Ns, cudaMemcpyDeviceToHost, s.st));
       PF_CU(cudaStreamSynchronize(s.st));
-      for (long i = 0; i < s.ng; ++i) out[i] = t[i];
+      double L = 0.0;
+      for (int k = 0; k < nlog; ++k) L += l[k];
+      const double f = std::exp(-L);
+      for (long i = 0; i < s.ng; ++i) out[i] = (double)t[i] * f;
     }
   });
 }
@@ -1460,6 +1520,25 @@ int pf_last_timing(const pf_system* sys, double* propagate_ms, double* density_m
   if (mde_steps) *mde_steps = sys->s->mde_steps;
   return PF_OK;
 }
+int pf_record_event(pf_system* sys, int slot) {
+  return guard(sys, [&](pf::System& s) {
+    if (slot < 0 || slot >= 8) throw pf::PFError(PF_EARG, "event slot must be in [0, 8)");
+    PF_CU(cudaEventRecord(s.uev[slot], s.st));
+  });
+}
+
+int pf_elapsed_ms(pf_system* sys, int a, int b, double* ms) {
+  return guard(sys, [&](pf::System& s) {
+    if (a < 0 || a >= 8 || b < 0 || b >= 8 || !ms) throw pf::PFError(PF_EARG, "bad event slots");
+    PF_CU(cudaEventSynchronize(s.uev[b]));
+    float v = 0.f;
+    PF_CU(cudaEventElapsedTime(&v, s.uev[a], s.uev[b]));
+    *ms = v;
+  });
+}
+
+long pf_launch_count(void) { return pf::launch_total(); }
+
 int pf_synchronize(pf_system* sys) {
   return guard(sys, [&](pf::System& s) { PF_CU(cudaStreamSynchronize(s.st)); });
 }

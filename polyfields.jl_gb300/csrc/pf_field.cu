@@ -9,9 +9,15 @@
 // All system-level grids are FP64: fields w, potentials, residuals and densities are
 // nmon consecutive grids of Ng.  Sums over the grid are deterministic: each CTA writes a
 // partial, a second kernel adds the partials in a fixed order.
+#include <atomic>
+
 #include "pf_kernels.h"
 
 namespace pf {
+
+static std::atomic<long> g_launches{0};
+void count_launches(long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long launch_total() { return g_launches.load(std::memory_order_relaxed); }
 
 static int red_blocks(long n) {
   long b = (n + 255) / 256;
@@ -33,6 +39,7 @@ __global__ void reduce_parts_kernel(const double* __restrict__ part, int nblk, i
 
 static void reduce_parts(const double* part, int nblk, int nval, double* out, double div, cudaStream_t st) {
   reduce_parts_kernel<<<nval, 256, 0, st>>>(part, nblk, nval, out, div);
+  count_launches(1);
 }
 
 // ------------------------------------------------------------------ plain sums
@@ -50,6 +57,7 @@ template <typename T>
 void launch_sum(const T* a, long n, double* part, double* out, double div, cudaStream_t st) {
   const int nb = red_blocks(n);
   sum_kernel<T><<<nb, 256, 0, st>>>(a, n, part);
+  count_launches(1);
   reduce_parts(part, nb, 1, out, div, st);
 }
 template void launch_sum<float>(const float*, long, double*, double*, double, cudaStream_t);
@@ -68,6 +76,7 @@ __global__ void point_q_kernel(const double* __restrict__ w, double vol, long n,
 void launch_point_q(const double* w, double vol, long n, double* part, double* Qdev, cudaStream_t st) {
   const int nb = red_blocks(n);
   point_q_kernel<<<nb, 256, 0, st>>>(w, vol, n, part);
+  count_launches(1);
   reduce_parts(part, nb, 1, Qdev, (double)n, st);
 }
 
@@ -81,6 +90,7 @@ __global__ void point_density_kernel(double* __restrict__ rho, const double* __r
 void launch_point_density(double* rho, const double* w, double vol, double phi, const double* Qdev, long n,
                           cudaStream_t st) {
   point_density_kernel<<<red_blocks(n), 256, 0, st>>>(rho, w, vol, phi, Qdev, n);
+  count_launches(1);
 }
 
 // ------------------------------------------------------------------ Simpson density
@@ -89,14 +99,14 @@ void launch_point_density(double* rho, const double* w, double vol, double phi, 
 template <typename T>
 __global__ void simpson_kernel(double* __restrict__ rho_all, const T* __restrict__ q, const T* __restrict__ qc,
                                bool rev, int Ns, long ng, SimpsonBlocks blk, double phi, double Nref,
-                               const double* __restrict__ Qdev) {
-  const double QN = (*Qdev) * Nref;
+                               const double* __restrict__ Qdev, const double* __restrict__ fac) {
+  const double QN = fac ? Nref : (*Qdev) * Nref;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ng; i += (long)gridDim.x * blockDim.x) {
     double bval[kMaxMon * 2];
     for (int b = 0; b < blk.nblocks; ++b) {
       const int s0 = blk.bgn[b], s1 = blk.end[b];
 #define PF_QC(s) ((double)(rev ? q[(long)(Ns - (s)) * ng + i] : qc[(long)(s) * ng + i]))
-#define PF_Q(s) ((double)q[(long)(s) * ng + i])
+#define PF_Q(s) ((double)q[(long)(s) * ng + i] * (fac ? fac[s] : 1.0))
       double acc = PF_Q(s0) * PF_QC(s0);
       acc += PF_Q(s1) * PF_QC(s1);
       for (int s = s0 + 1; s < s1; s += 2) acc += 4.0 * PF_Q(s) * PF_QC(s);
@@ -121,15 +131,49 @@ __global__ void simpson_kernel(double* __restrict__ rho_all, const T* __restrict
 
 template <typename T>
 void launch_simpson(double* rho_all, const T* q, const T* qc, bool qc_reversed, int Ns, long ng,
-                    const SimpsonBlocks& blk, double phi, double Nref, const double* Qdev, cudaStream_t st) {
+                    const SimpsonBlocks& blk, double phi, double Nref, const double* Qdev, const double* fac,
+                    cudaStream_t st) {
   int nb = (int)((ng + 255) / 256);
   if (nb > 8192) nb = 8192;
-  simpson_kernel<T><<<nb, 256, 0, st>>>(rho_all, q, qc, qc_reversed, Ns, ng, blk, phi, Nref, Qdev);
+  simpson_kernel<T><<<nb, 256, 0, st>>>(rho_all, q, qc, qc_reversed, Ns, ng, blk, phi, Nref, Qdev, fac);
+  count_launches(1);
 }
 template void launch_simpson<float>(double*, const float*, const float*, bool, int, long, const SimpsonBlocks&,
-                                    double, double, const double*, cudaStream_t);
+                                    double, double, const double*, const double*, cudaStream_t);
 template void launch_simpson<double>(double*, const double*, const double*, bool, int, long, const SimpsonBlocks&,
-                                     double, double, const double*, cudaStream_t);
+                                     double, double, const double*, const double*, cudaStream_t);
+
+__global__ void scale_finalize_kernel(const double* __restrict__ lf, const double* __restrict__ lb, bool rev, int Ns,
+                                      const double* __restrict__ meanq, double* __restrict__ Qdev,
+                                      double* __restrict__ fac) {
+  extern __shared__ double Lsh[];  // forward prefix L_s, s = 0..Ns, then backward L'_s
+  double* Lf = Lsh;
+  double* Lb = Lsh + (Ns + 1);
+  if (threadIdx.x == 0) {
+    Lf[0] = 0.0;
+    for (int t = 0; t < Ns; ++t) Lf[t + 1] = Lf[t] + lf[t];
+    if (rev) {
+      for (int s = 0; s <= Ns; ++s) Lb[s] = Lf[Ns - s];
+    } else {
+      Lb[Ns] = 0.0;
+      for (int t = 0; t < Ns; ++t) Lb[Ns - t - 1] = Lb[Ns - t] + lb[t];
+    }
+    const double logQ = log(*meanq) - Lf[Ns];
+    *Qdev = exp(logQ);
+    Lsh[2 * (Ns + 1)] = logQ;
+  }
+  __syncthreads();
+  const double logQ = Lsh[2 * (Ns + 1)];
+  for (int s = threadIdx.x; s <= Ns; s += blockDim.x) fac[s] = exp(-Lf[s] - Lb[s] - logQ);
+}
+
+void launch_scale_finalize(const double* lsc_fwd, const double* lsc_bwd, bool rev, int Ns, const double* meanq,
+                           double* Qdev, double* fac, cudaStream_t st) {
+  const size_t smem = sizeof(double) * (2 * (size_t)(Ns + 1) + 1);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(scale_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  scale_finalize_kernel<<<1, 256, smem, st>>>(lsc_fwd, lsc_bwd, rev, Ns, meanq, Qdev, fac);
+  count_launches(1);
+}
 
 // ------------------------------------------------------------------ residuals
 // pot_a = sum_b chi_ab rho_b / v_b ; eta = (sum rho - 1 + sum_a (w_a - pot_a)) / nmon ;
@@ -192,9 +236,11 @@ int launch_residuals(double* w, double* pot, double* res, const double* rho, con
                      bool canonical, double* part, double* sums, cudaStream_t st) {
   const int nb = red_blocks(ng);
   residual_kernel<<<nb, 256, 0, st>>>(w, pot, res, rho, ms, ng, part);
+  count_launches(1);
   if (canonical) {
     reduce_parts(part, nb, 2 * ms.nmon, sums, (double)ng, st);
     meansub_kernel<<<nb, 256, 0, st>>>(w, res, sums, ms.nmon, ng);
+  count_launches(1);
   }
   return OK;
 }
@@ -234,6 +280,7 @@ void launch_stats(const double* w, const double* res, const double* rho, const M
                   double* part, double* out4, cudaStream_t st) {
   const int nb = red_blocks(ng);
   stats_kernel<<<nb, 256, 0, st>>>(w, res, rho, ms, ng, part);
+  count_launches(1);
   reduce_parts(part, nb, 4, out4, 1.0, st);
 }
 
@@ -247,6 +294,7 @@ void launch_axpy(double* y, const double* x, double a, long n, cudaStream_t st) 
   int nb = (int)((n + 255) / 256);
   if (nb > 8192) nb = 8192;
   axpy_kernel<<<nb, 256, 0, st>>>(y, x, a, n);
+  count_launches(1);
 }
 
 // Gram sums over all monomer grids (n_all = nmon * Ng): with r = res[ih] and d_m = r - res[ih-m],
@@ -313,6 +361,7 @@ void launch_gram(const HistPtrs& h, int ih, long n_all, double* part, double* ou
   const size_t smem = sizeof(double) * (size_t)(ih + 1) * kGramTile;
   if (smem > 48 * 1024) cudaFuncSetAttribute(gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   gram_kernel<<<(int)nb, 256, smem, st>>>(h, ih, n_all, part);
+  count_launches(1);
   reduce_parts(part, (int)nb, nout, out, 1.0, st);
 }
 
@@ -410,6 +459,7 @@ void launch_solve(const double* packed, int ih, double* Cn, int* status, cudaStr
   const size_t smem = 2 * sizeof(double) * (size_t)ih * (ih + 1);
   if (smem > 48 * 1024) cudaFuncSetAttribute(solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   solve_kernel<<<1, 64, smem, st>>>(packed, ih, Cn, status);
+  count_launches(1);
 }
 
 // w = W + lam D,  W = w + sum_nn Cn[nn-1] (f[ih-nn] - f[ih]),  D = r + sum_nn Cn[nn-1] (r[ih-nn] - r)
@@ -435,6 +485,7 @@ void launch_mix(double* w, const HistPtrs& h, int ih, const double* Cn, double l
   int nb = (int)((n_all + 255) / 256);
   if (nb > 8192) nb = 8192;
   mix_kernel<<<nb, 256, 0, st>>>(w, h, ih, Cn, lam, n_all);
+  count_launches(1);
 }
 
 }  // namespace pf

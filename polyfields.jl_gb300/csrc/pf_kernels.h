@@ -28,11 +28,17 @@ struct StepOp {
 };
 
 // One chain propagation: hist[s] for s = s0, s0+dir, ..., s0+dir*nsteps.
+// With csc/lsc set, step t is rescaled by the factor c_t = Ng / sum(LW * q_t) (the k = 0
+// term of the forward transform), so the stored histories stay O(1) in float32; csc[t] is
+// the float factor applied and lsc[t] = log(c_t) in float64.  The stored q_s is then the
+// true propagator times exp(sum_{t<s} lsc[t]).
 template <typename T>
 struct ChainJob {
   T* hist;
   const StepOp<T>* ops;  // nsteps entries
   Cx<T>* kbuf;           // 3D grids: half-spectrum scratch of Nk complex
+  float* csc;            // nsteps rescale factors, or null (no rescaling)
+  double* lsc;           // nsteps log factors
   int s0, dir, nsteps, pad;
 };
 
@@ -61,6 +67,10 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   __syncthreads();
   return r;
 }
+
+// Number of kernels this library has launched (all handles), for launch accounting.
+void count_launches(long n);
+long launch_total();
 
 // ---- propagator launchers (pf_mde_impl.cuh, instantiated in pf_mde_fp32.cu / pf_mde_fp64.cu)
 // Pencils per tile of the z pass (128-byte rows): 16 for float32, 8 for float64.
@@ -104,9 +114,17 @@ void launch_sum(const T* a, long n, double* part, double* out, double div, cudaS
 void launch_point_q(const double* w, double vol, long n, double* part, double* Qdev, cudaStream_t st);
 void launch_point_density(double* rho, const double* w, double vol, double phi, const double* Qdev, long n,
                           cudaStream_t st);
+// fac (optional, Ns+1 entries) multiplies each contour term: rescaled histories pass
+// fac[s] = exp(-L_s - L'_s - log Q) and the kernel then skips the division by Q.
 template <typename T>
 void launch_simpson(double* rho_all, const T* q, const T* qc, bool qc_reversed, int Ns, long ng,
-                    const SimpsonBlocks& blk, double phi, double Nref, const double* Qdev, cudaStream_t st);
+                    const SimpsonBlocks& blk, double phi, double Nref, const double* Qdev, const double* fac,
+                    cudaStream_t st);
+// Q and the Simpson factors of a rescaled chain: L_s = sum_{t<s} lsc_fwd[t],
+// L'_s = sum_{t<Ns-s} lsc_bwd[t] (or L_{Ns-s} when rev), log Q = log(meanq) - L_Ns,
+// fac[s] = exp(-L_s - L'_s - log Q).  One block.
+void launch_scale_finalize(const double* lsc_fwd, const double* lsc_bwd, bool rev, int Ns, const double* meanq,
+                           double* Qdev, double* fac, cudaStream_t st);
 int launch_residuals(double* w, double* pot, double* res, const double* rho, const MonomerSet& ms, long ng,
                      bool canonical, double* part, double* sums, cudaStream_t st);
 void launch_stats(const double* w, const double* res, const double* rho, const MonomerSet& ms, long ng,

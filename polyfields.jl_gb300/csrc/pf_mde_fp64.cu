@@ -8,6 +8,7 @@ void launch_dksq(double* dk, const CellGeom& g, int nparams, long nk, cudaStream
   int blocks = (int)((nk + 255) / 256);
   if (blocks > 4096) blocks = 4096;
   dksq_kernel<<<blocks, 256, 0, st>>>(dk, g, nparams);
+  count_launches(1);
 }
 
 }  // namespace pf

@@ -94,6 +94,14 @@ __global__ void fill_kernel(T* __restrict__ a, T v, long n) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) a[i] = v;
 }
 
+// Rescale factor of one contour step: 1 / mean(LW * q_t), from the grid sum dc (the k = 0
+// coefficient of the forward transform); 1 when that mean is not a positive finite number.
+template <typename T>
+__device__ __forceinline__ T rescale_factor(T dc, double n) {
+  const double m = (double)dc / n;
+  return (m > 0.0 && isfinite(m)) ? (T)(1.0 / m) : (T)1;
+}
+
 // ------------------------------------------------------------------ plane helpers
 // Write u = lw * q (or q when lw is null) into the pair layout of S.
 template <typename T, int NX, int NY>
@@ -110,12 +118,12 @@ __device__ __forceinline__ void load_plane(Cx<T>* S, const T* __restrict__ lw, c
 // given put u = lw_next * q_out back into S for the next step.
 template <typename T, int NX, int NY>
 __device__ __forceinline__ void finish_plane(Cx<T>* S, const T* __restrict__ lw_cur, const T* __restrict__ lw_next,
-                                             T* __restrict__ qout) {
+                                             T* __restrict__ qout, T cscale) {
   using C = PlaneCfg<NX, NY>;
   for (int i = threadIdx.x; i < C::NP; i += blockDim.x) {
     const int y = i / NX, x = i - y * NX;
     T& e = pair_elem(S, C::KX, y, x);
-    const T qv = lw_cur[i] * e;
+    const T qv = lw_cur[i] * (e * cscale);
     qout[i] = qv;
     if (lw_next) {
       e = lw_next[i] * qv;
@@ -140,15 +148,24 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
       __syncthreads();
     }
     plane_fwd<T, NX, NY>(S, tw.x, tw.y);
+    T c = (T)1;
+    if (job.csc) {
+      c = rescale_factor<T>(S[0].x, (double)C::NP);
+      if (threadIdx.x == 0) {
+        job.csc[t] = (float)c;
+        job.lsc[t] = log((double)c);
+      }
+      __syncthreads();  // every thread has read S[0] before it is overwritten below
+    }
     for (int k = threadIdx.x; k < C::NKP; k += blockDim.x) {
-      const T f = op.ld[k];
+      const T f = op.ld[k] * c;
       S[k] = cx<T>(S[k].x * f, S[k].y * f);
     }
     __syncthreads();
     plane_inv<T, NX, NY>(S, tw.x, tw.y);
     const int s_out = job.s0 + job.dir * (t + 1);
     const T* lw_next = (t + 1 < job.nsteps) ? job.ops[t + 1].lw : nullptr;
-    finish_plane<T, NX, NY>(S, op.lw, lw_next, job.hist + (long)s_out * C::NP);
+    finish_plane<T, NX, NY>(S, op.lw, lw_next, job.hist + (long)s_out * C::NP, (T)1);
     __syncthreads();
   }
 }
@@ -174,7 +191,8 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
     const StepOp<T> op = job.ops[t - 1];
     const int s_out = job.s0 + job.dir * t;
     const T* lw_next = start ? job.ops[t].lw + (long)z * C::NP : nullptr;
-    finish_plane<T, NX, NY>(S, op.lw + (long)z * C::NP, lw_next, job.hist + (long)s_out * ng + (long)z * C::NP);
+    const T c = job.csc ? (T)job.csc[t - 1] : (T)1;
+    finish_plane<T, NX, NY>(S, op.lw + (long)z * C::NP, lw_next, job.hist + (long)s_out * ng + (long)z * C::NP, c);
   } else {
     load_plane<T, NX, NY>(S, job.ops[0].lw + (long)z * C::NP, job.hist + (long)job.s0 * ng + (long)z * C::NP);
   }
@@ -195,7 +213,7 @@ struct ZCfg {
 
 template <typename T, int NZ>
 __global__ void __launch_bounds__(512)
-    z_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nkp, Twiddles<T> tw) {
+    z_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nkp, double ng, Twiddles<T> tw) {
   constexpr int M = ZCfg<T>::M;
   constexpr int TOT = NZ * M;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -212,6 +230,12 @@ __global__ void __launch_bounds__(512)
   __syncthreads();
   fft_batch_n<T, false, NZ>(Tl, M, 1, M, tw.z);
   __syncthreads();
+  if (job.csc && blockIdx.x == 0 && threadIdx.x == 0) {
+    // the (0, 0, 0) coefficient is the grid sum of LW * q_t
+    const T c = rescale_factor<T>(Tl[0].x, ng);
+    job.csc[t] = (float)c;
+    job.lsc[t] = log((double)c);
+  }
   const T* ld = job.ops[t].ld;
   for (int i = threadIdx.x; i < TOT; i += blockDim.x) {
     const int zz = i / M, mm = i - zz * M;
@@ -340,7 +364,7 @@ static int z_threads() {
 }
 
 template <typename T, int NZ>
-static void launch_z_step(const ChainJob<T>* jobs, int t, int nkp, int njobs, const Twiddles<T>& tw,
+static void launch_z_step(const ChainJob<T>* jobs, int t, int nkp, double ng, int njobs, const Twiddles<T>& tw,
                           cudaStream_t st) {
   constexpr int M = ZCfg<T>::M;
   const size_t sz = sizeof(Cx<T>) * (size_t)NZ * M;
@@ -350,16 +374,18 @@ static void launch_z_step(const ChainJob<T>* jobs, int t, int nkp, int njobs, co
     attr = true;
   }
   const int ntiles = (nkp + M - 1) / M;
-  z_step_kernel<T, NZ><<<dim3(ntiles, njobs), z_threads<T>(), sz, st>>>(jobs, t, nkp, tw);
+  z_step_kernel<T, NZ><<<dim3(ntiles, njobs), z_threads<T>(), sz, st>>>(jobs, t, nkp, ng, tw);
+    count_launches(1);
 }
 
 template <typename T>
-static bool z_step_dispatch(int nz, const ChainJob<T>* jobs, int t, int nkp, int njobs, const Twiddles<T>& tw,
+static bool z_step_dispatch(int nz, const ChainJob<T>* jobs, int t, int nkp, double ng, int njobs,
+                            const Twiddles<T>& tw,
                             cudaStream_t st) {
   switch (nz) {
 #define PF_Z(N)                                           \
   case N:                                                 \
-    launch_z_step<T, N>(jobs, t, nkp, njobs, tw, st);     \
+    launch_z_step<T, N>(jobs, t, nkp, ng, njobs, tw, st); \
     return true;
     PF_Z_LENGTHS(PF_Z)
 #undef PF_Z
@@ -381,11 +407,13 @@ static void chains_shape(const ChainJob<T>* jobs, int njobs, int maxsteps, int n
   }
   if (nz == 1) {
     chain_plane_kernel<T, NX, NY><<<njobs, C::THREADS, sp, st>>>(jobs, tw);
+    count_launches(1);
     return;
   }
   for (int t = 0; t <= maxsteps; ++t) {
     xy_step_kernel<T, NX, NY><<<dim3(nz, njobs), C::THREADS, sp, st>>>(jobs, t, nz, tw);
-    if (t < maxsteps) z_step_dispatch<T>(nz, jobs, t, C::NKP, njobs, tw, st);
+    count_launches(1);
+    if (t < maxsteps) z_step_dispatch<T>(nz, jobs, t, C::NKP, (double)C::NP * nz, njobs, tw, st);
   }
 }
 
@@ -404,10 +432,13 @@ static void stress_shape(const StressItem<T>* items, int nitems, const T* const*
   }
   if (nz == 1) {
     stress_plane_kernel<T, NX, NY><<<nitems, C::THREADS, ss, st>>>(items, dksq, nparams, part, tw);
+    count_launches(1);
     return;
   }
   xy_fwd_kernel<T, NX, NY><<<dim3(nz, nitems), C::THREADS, sp, st>>>(src_q, kq, tw);
+    count_launches(1);
   xy_fwd_kernel<T, NX, NY><<<dim3(nz, nitems), C::THREADS, sp, st>>>(src_qc, kqc, tw);
+    count_launches(1);
   constexpr int M = ZCfg<T>::M;
   const int ntiles = (C::NKP + M - 1) / M;
   switch (nz) {
@@ -419,7 +450,7 @@ static void stress_shape(const StressItem<T>* items, int nitems, const T* const*
       set_smem(z_fwd_stress_kernel<T, N>, sz);                                                               \
       za = true;                                                                                             \
     }                                                                                                        \
-    z_fwd_stress_kernel<T, N><<<dim3(ntiles, nitems), 256, sz, st>>>(kq, kqc, C::NKP, dksq, nparams, part, tw); \
+    z_fwd_stress_kernel<T, N><<<dim3(ntiles, nitems), 256, sz, st>>>(kq, kqc, C::NKP, dksq, nparams, part, tw); count_launches(1); \
   } break;
     PF_Z_LENGTHS(PF_Z)
 #undef PF_Z
@@ -450,6 +481,7 @@ void launch_lw(T* lw, const double* w, double coeff, long n, cudaStream_t st) {
   int blocks = (int)((n + 255) / 256);
   if (blocks > 4096) blocks = 4096;
   lw_kernel<T><<<blocks, 256, 0, st>>>(lw, w, coeff, n);
+    count_launches(1);
 }
 
 template <typename T>
@@ -457,6 +489,7 @@ void launch_ld(T* ld, const CellGeom& g, double coeff, double scale, long nk, cu
   int blocks = (int)((nk + 255) / 256);
   if (blocks > 4096) blocks = 4096;
   ld_kernel<T><<<blocks, 256, 0, st>>>(ld, g, coeff, scale);
+    count_launches(1);
 }
 
 template <typename T>
@@ -464,6 +497,7 @@ void launch_fill(T* a, T v, long n, cudaStream_t st) {
   int blocks = (int)((n + 255) / 256);
   if (blocks > 4096) blocks = 4096;
   fill_kernel<T><<<blocks, 256, 0, st>>>(a, v, n);
+    count_launches(1);
 }
 
 template <typename T>

@@ -69,6 +69,9 @@ SIGNATURES = {
     "pf_propagate": (_c_int, [_vp, _dptr, _c_double, _c_double, _c_double, _dptr, _dptr, _c_int]),
     "pf_set_timing": (_c_int, [_vp, _c_int]),
     "pf_last_timing": (_c_int, [_vp, _dptr, _dptr, _iptr]),
+    "pf_record_event": (_c_int, [_vp, _c_int]),
+    "pf_elapsed_ms": (_c_int, [_vp, _c_int, _c_int, _dptr]),
+    "pf_launch_count": (ctypes.c_long, []),
     "pf_synchronize": (_c_int, [_vp]),
 }
 

@@ -1,0 +1,98 @@
+"""Workload builders: the benchmark and test systems, with seeded synthetic fields.
+
+Each builder takes an API module as its first argument -- this package, or any module that
+exposes the reference's names (Monomer, Diblock, UnitCell, FieldSystem, FloryInteraction,
+fieldinit) -- and returns a system whose fields were injected with fieldinit(sys, Dict)
+semantics (src/fileio.jl:25-54).  Inputs are NumPy PCG64 streams, so every caller builds
+bit-identical fields.
+"""
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "tests", "golden")
+
+
+def _fs(M, dims, cell, mons, precision):
+    if precision is None:
+        return M.FieldSystem(dims, cell, monomers=mons)
+    return M.FieldSystem(dims, cell, monomers=mons, precision=precision)
+
+
+def seeded_fields(shape, mids, seed=12345, scale=0.1, pattern=None):
+    """Seeded Gaussian noise (NumPy PCG64) plus an optional ordered pattern for mids[0] and
+    its negative for mids[1]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = {m: scale * rng.standard_normal(shape) for m in mids}
+    if pattern is not None:
+        out[mids[0]] = out[mids[0]] + pattern
+        out[mids[1]] = out[mids[1]] - pattern
+    return out
+
+
+def diblock_system(M, dims, crystal, params, N=100, f=0.5, chi=0.2, Ns=100, precision=None, seed=12345,
+                   scale=0.1, amp=0.5):
+    A, B = M.Monomer(1, 1.0), M.Monomer(2, 1.0)
+    cell = M.UnitCell(sum(1 for d in dims if d > 1), crystal, *params)
+    sys = _fs(M, dims, cell, [A, B], precision)
+    sys.add_species(M.Diblock(A, B, N, f, 1.0, 1.0, Ns), 1.0)
+    itx = M.FloryInteraction()
+    itx.set_interaction(A, B, chi)
+    sys.add_interaction(itx)
+    shape = (dims[2], dims[1], dims[0])
+    z, y, x = np.meshgrid(*(np.arange(n) / n for n in shape), indexing="ij")
+    pattern = amp * (np.cos(2 * np.pi * x) + (np.cos(2 * np.pi * y) if dims[1] > 1 else 0)
+                     + (np.cos(2 * np.pi * z) if dims[2] > 1 else 0))
+    M.fieldinit(sys, seeded_fields(shape, [1, 2], seed, scale, pattern))
+    return sys
+
+
+def blend_seed_system(M, precision=None):
+    """examples/seeds/abc_blend_1d.json with the notebook's blend (examples.ipynb cell 11)."""
+    d = np.load(os.path.join(GOLDEN, "seed_abc_blend_1d.npz"))
+    A, B, C = M.Monomer(1, 2.0), M.Monomer(2, 2.0), M.Monomer(3, 1.0)
+    cell = M.UnitCell(int(d["dim"]), str(d["crystal"]), *d["cell_params"])
+    sys = _fs(M, tuple(int(g) for g in d["grid"]), cell, [A, B, C], precision)
+    sys.add_species(M.Point(C), 0.4)
+    sys.add_species(M.Homopolymer(A, 100, 1.0), 0.3)
+    sys.add_species(M.Homopolymer(B, 100, 1.0), 0.3)
+    itx = M.FloryInteraction()
+    itx.set_interaction(A, B, 0.5)
+    itx.set_interaction(A, C, 1.25)
+    itx.set_interaction(B, C, 1.25)
+    sys.add_interaction(itx)
+    M.fieldinit(sys, {int(k[1:]): d[k] for k in d.files if k.startswith("w")})
+    return sys
+
+
+def cyl2d_seed_system(M, precision=None):
+    """examples/seeds/cyl2d.json with the notebook's cylinder system (examples.ipynb cell 7)."""
+    d = np.load(os.path.join(GOLDEN, "seed_cyl2d.npz"))
+    A, B = M.Monomer(1), M.Monomer(2)
+    cell = M.UnitCell(2, "hexagonal", *d["cell_params"])
+    sys = _fs(M, tuple(int(g) for g in d["grid"]), cell, [A, B], precision)
+    sys.add_species(M.Diblock(A, B, 100, 0.3, 1.0, 1.0, 100), 1.0)
+    itx = M.FloryInteraction()
+    itx.set_interaction(A, B, 0.3)
+    sys.add_interaction(itx)
+    M.fieldinit(sys, {int(k[1:]): d[k] for k in d.files if k.startswith("w")})
+    return sys
+
+
+def blend3d_system(M, n=32, L=14.0, precision=None, Ns=200, seed=12345):
+    """The large-blend workload (128^3 at full size): AB diblock N100 fA0.4 (phi 0.8) + A
+    homopolymer N50 (phi 0.2), chi 0.2, Ns 200, cubic cell L0 = 14, double-gyroid start
+    w_A = sin x cos y + sin y cos z + sin z cos x (x = 2 pi X / L), w_B = -w_A, + 0.05 noise."""
+    A, B = M.Monomer(1), M.Monomer(2)
+    cell = M.UnitCell(3, "cubic", L)
+    sys = _fs(M, (n, n, n), cell, [A, B], precision)
+    sys.add_species(M.Diblock(A, B, 100, 0.4, 1.0, 1.0, Ns), 0.8)
+    sys.add_species(M.Homopolymer(A, 50, 1.0, Ns), 0.2)
+    itx = M.FloryInteraction()
+    itx.set_interaction(A, B, 0.2)
+    sys.add_interaction(itx)
+    shape = (n, n, n)
+    z, y, x = np.meshgrid(*(2 * np.pi * np.arange(n) / n for _ in range(3)), indexing="ij")
+    gyr = np.sin(x) * np.cos(y) + np.sin(y) * np.cos(z) + np.sin(z) * np.cos(x)
+    M.fieldinit(sys, seeded_fields(shape, [1, 2], seed, 0.05, gyr))
+    return sys

@@ -218,3 +218,28 @@ def test_singular_gram_raises():
     u.step()
     with pytest.raises(pf.PolyFieldsError, match="Error inverting Umn"):
         u.step()
+
+
+def test_fp32_rescaled_strong_fields():
+    """Strong double-gyroid fields make Q ~ 1e40+, beyond float32's range: the FP32 chains
+    are rescaled per contour step and the factors are carried in FP64 (Q, density, stress)."""
+    o = SY.blend3d_system(O, n=16)
+    g = SY.blend3d_system(pf, n=16, precision="fp32")
+    assert o.species[0].Q > 1e30
+    for isp in range(2):
+        assert g.species[isp].Q == pytest.approx(o.species[isp].Q, rel=FP32_RTOL)
+    for mid in (1, 2):
+        assert rel(g.density[mid], o.density[mid]) < 2 * FP32_RTOL
+    assert g.free_energy() == pytest.approx(o.free_energy(), rel=1e-5)
+    assert np.allclose(g.scfstress(), o.scfstress(), rtol=2e-3, atol=1e-9)
+
+
+def test_fp32_propagator_accessor_unscaled():
+    """chain.q[s] / qc[s] read back from rescaled FP32 histories equal the true propagators."""
+    kw = dict(dims=(32, 32, 1), crystal="hexagonal", params=(9.0,), f=0.3, chi=0.3)
+    o = SY.diblock_system(O, **kw)
+    g = SY.diblock_system(pf, precision="fp32", **kw)
+    ch_o, ch_g = o.species[0], g.species[0]
+    for s in (0, 7, 50, ch_o.Ns):
+        assert rel(ch_g.propagator(s), ch_o.q[s]) < FP32_RTOL
+        assert rel(ch_g.propagator(s, conjugate=True), ch_o.qc[s]) < FP32_RTOL
