@@ -100,11 +100,11 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline_sample(nsteps=80):
+def cpu_baseline_sample(min_seconds=10.0):
     """The FP64 CPU restatement (oracle, NumPy + pocketfft on all cores) on a bounded sample of
-    the same workload: nsteps contour steps of the 128^3 propagator, scaled to one SCFT
-    iteration (600 contour steps).  The Simpson integration and the Anderson update are not in
-    the sample, so the CPU rate is an upper bound."""
+    the same workload: contour steps of the 128^3 propagator for at least min_seconds, scaled
+    to one SCFT iteration (600 contour steps).  The Simpson integration and the Anderson
+    update are not in the sample, so the CPU rate is an upper bound."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import pf_oracle as O
@@ -120,9 +120,11 @@ def cpu_baseline_sample(nsteps=80):
     out = np.empty_like(q)
     solver.propagate(q, out)
     t0 = time.perf_counter()
-    for _ in range(nsteps):
+    nsteps = 0
+    while nsteps < 10 or time.perf_counter() - t0 < min_seconds:
         solver.propagate(q, out)
         q, out = out, q
+        nsteps += 1
     dt = time.perf_counter() - t0
     return {"value": (nsteps / dt) / MDE_STEPS_PER_ITER, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
             "sample": f"{nsteps} contour steps of the 128^3 FP64 propagator (NumPy/pocketfft, FFTs on all cores, "
@@ -148,7 +150,7 @@ def run_reference(args):
     solver.update(0.05 * rng.standard_normal(solver.shape), cell.ksq, 1.0, 1.0, 0.5)
     q = np.ones(solver.shape)
     out = np.empty_like(q)
-    per_step = 20
+    per_step = 100
 
     def one():
         nonlocal q, out
@@ -268,7 +270,7 @@ def run_gpu(args):
         fp64 = {"iters_per_s": 1000.0 * args.fp64_steps / m64.value, "ms_per_iter": m64.value / args.fp64_steps,
                 "mde_step_us": 1000.0 * a64 / nmde}
 
-    cpu = cpu_baseline_sample(args.cpu_steps) if args.cpu_steps > 0 else None
+    cpu = cpu_baseline_sample(args.cpu_seconds) if args.cpu_seconds > 0 else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 propagators + f64 reductions", "data": "synthetic", "config": dict(WORKLOAD, size=n),
@@ -289,7 +291,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=N_GRID, help="grid points per axis (default 128)")
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--cpu-steps", type=int, default=80, help="contour steps of the CPU baseline sample (0: skip)")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="length of the CPU baseline sample (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -96,24 +96,108 @@ void launch_point_density(double* rho, const double* w, double vol, double phi, 
 // ------------------------------------------------------------------ Simpson density
 // rho_all[mon*ng + i] += phi * sum_{blocks of mon} (ds/3) * S_blk(i) / (Q * Nref), with
 // S_blk = q_b qc_b + q_e qc_e + 4 sum_odd q qc + 2 sum_even q qc in the reference's order.
+// Each thread integrates W consecutive grid points (one 16-byte vector of T per contour
+// point and chain), keeping the reference's summation order per point; the s loops are
+// unrolled so several vector loads are in flight per thread.
 template <typename T>
-__global__ void simpson_kernel(double* __restrict__ rho_all, const T* __restrict__ q, const T* __restrict__ qc,
-                               bool rev, int Ns, long ng, SimpsonBlocks blk, double phi, double Nref,
-                               const double* __restrict__ Qdev, const double* __restrict__ fac) {
+struct Vec;
+template <>
+struct Vec<float> {
+  __device__ static float get(const float4& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+};
+template <>
+struct Vec<double> {
+  __device__ static double get(const double2& v, int k) { return k == 0 ? v.x : v.y; }
+};
+
+template <typename T>
+struct SimpVec;
+template <>
+struct SimpVec<float> {
+  using V = float4;
+  static constexpr int W = 4;
+  __device__ static void unpack(const V& v, double* o) {
+    o[0] = v.x;
+    o[1] = v.y;
+    o[2] = v.z;
+    o[3] = v.w;
+  }
+};
+template <>
+struct SimpVec<double> {
+  using V = double2;
+  static constexpr int W = 2;
+  __device__ static void unpack(const V& v, double* o) {
+    o[0] = v.x;
+    o[1] = v.y;
+  }
+};
+
+// Accumulator of one Simpson sum: float64 for float64 histories (the reference's arithmetic);
+// for float32 histories a compensated (Kahan) float32 sum, converted to float64 once per
+// block -- GB300 runs float64 at 1/57 of the float32 rate, so per-term float64 work would
+// dominate this memory-bound pass.
+template <typename T>
+struct SimpAcc {
+  double s;
+  __device__ void init(double v) { s = v; }
+  __device__ void add(double v) { s += v; }
+  __device__ double value() const { return s; }
+};
+template <>
+struct SimpAcc<float> {
+  float s, c;
+  __device__ void init(float v) {
+    s = v;
+    c = 0.f;
+  }
+  __device__ void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ double value() const { return (double)s - (double)c; }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) simpson_kernel(double* __restrict__ rho_all, const T* __restrict__ q,
+                                                      const T* __restrict__ qc, bool rev, int Ns, long ng,
+                                                      SimpsonBlocks blk, double phi, double Nref,
+                                                      const double* __restrict__ Qdev, const double* __restrict__ fac) {
+  using SV = SimpVec<T>;
+  using V = typename SV::V;
+  constexpr int W = SV::W;
   const double QN = fac ? Nref : (*Qdev) * Nref;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ng; i += (long)gridDim.x * blockDim.x) {
-    double bval[kMaxMon * 2];
+  const long nv = ng / W;
+  const V* q4 = reinterpret_cast<const V*>(q);
+  const V* qc4 = reinterpret_cast<const V*>(rev ? q : qc);
+  for (long iv = blockIdx.x * (long)blockDim.x + threadIdx.x; iv < nv; iv += (long)gridDim.x * blockDim.x) {
+    double bval[kMaxMon * 2][W];
     for (int b = 0; b < blk.nblocks; ++b) {
       const int s0 = blk.bgn[b], s1 = blk.end[b];
-#define PF_QC(s) ((double)(rev ? q[(long)(Ns - (s)) * ng + i] : qc[(long)(s) * ng + i]))
-#define PF_Q(s) ((double)q[(long)(s) * ng + i] * (fac ? fac[s] : 1.0))
-      double acc = PF_Q(s0) * PF_QC(s0);
-      acc += PF_Q(s1) * PF_QC(s1);
-      for (int s = s0 + 1; s < s1; s += 2) acc += 4.0 * PF_Q(s) * PF_QC(s);
-      for (int s = s0 + 2; s < s1 - 1; s += 2) acc += 2.0 * PF_Q(s) * PF_QC(s);
-#undef PF_QC
-#undef PF_Q
-      bval[b] = (acc * (blk.ds[b] / 3.0)) / QN;
+      SimpAcc<T> acc[W];
+      auto term = [&](int s, T wgt, bool first) {
+        const long sc = rev ? (long)(Ns - s) : (long)s;
+        const V a = q4[(long)s * nv + iv];
+        const V c = qc4[sc * nv + iv];
+        const T f = fac ? (T)fac[s] : (T)1;
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+          const T ak = Vec<T>::get(a, k), ck = Vec<T>::get(c, k);
+          const T v = wgt == (T)1 ? (ak * f) * ck : wgt * (ak * f) * ck;
+          if (first) acc[k].init(v);
+          else acc[k].add(v);
+        }
+      };
+      term(s0, (T)1, true);
+      term(s1, (T)1, false);
+#pragma unroll 4
+      for (int s = s0 + 1; s < s1; s += 2) term(s, (T)4, false);
+#pragma unroll 4
+      for (int s = s0 + 2; s < s1 - 1; s += 2) term(s, (T)2, false);
+#pragma unroll
+      for (int k = 0; k < W; ++k) bval[b][k] = (acc[k].value() * (blk.ds[b] / 3.0)) / QN;
     }
     // pool blocks by monomer (block order), then add phi * species density
     unsigned done = 0;
@@ -121,10 +205,13 @@ __global__ void simpson_kernel(double* __restrict__ rho_all, const T* __restrict
       const int m = blk.mon[b];
       if (done & (1u << m)) continue;
       done |= 1u << m;
-      double dens = 0.0;
-      for (int c = b; c < blk.nblocks; ++c)
-        if (blk.mon[c] == m) dens += bval[c];
-      rho_all[(long)m * ng + i] += phi * dens;
+#pragma unroll
+      for (int k = 0; k < W; ++k) {
+        double dens = 0.0;
+        for (int c = b; c < blk.nblocks; ++c)
+          if (blk.mon[c] == m) dens += bval[c][k];
+        rho_all[(long)m * ng + iv * W + k] += phi * dens;
+      }
     }
   }
 }
@@ -133,7 +220,8 @@ template <typename T>
 void launch_simpson(double* rho_all, const T* q, const T* qc, bool qc_reversed, int Ns, long ng,
                     const SimpsonBlocks& blk, double phi, double Nref, const double* Qdev, const double* fac,
                     cudaStream_t st) {
-  int nb = (int)((ng + 255) / 256);
+  const long nv = ng / SimpVec<T>::W;
+  int nb = (int)((nv + 255) / 256);
   if (nb > 8192) nb = 8192;
   simpson_kernel<T><<<nb, 256, 0, st>>>(rho_all, q, qc, qc_reversed, Ns, ng, blk, phi, Nref, Qdev, fac);
   count_launches(1);

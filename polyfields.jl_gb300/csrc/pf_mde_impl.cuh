@@ -38,9 +38,14 @@ struct PlaneCfg {
   static constexpr int NP = NX * NY;                  // real points of a plane
   static constexpr int SLOTS = KX * (NY > 1 ? NY : 2);  // complex slots of the work plane
   static constexpr int THREADS = NY == 1 ? 32 : (NKP >= 4096 ? 512 : (NKP >= 1024 ? 256 : 128));
+  // float32 planes of >= 4096 spectral points: two CTAs per SM fit the shared memory, so ask
+  // the register allocator for that occupancy
+  static constexpr int MINB = NKP >= 4096 ? 2 : 1;
 };
 
 // ------------------------------------------------------------------ operator setup
+// LW = exp(-coeff * w) evaluated in float64 and rounded once to T: the propagator multiplies
+// by LW twice per contour step, so a biased float32 exp would compound over the chain.
 template <typename T>
 __global__ void lw_kernel(T* __restrict__ lw, const double* __restrict__ w, double coeff, long n) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
@@ -102,51 +107,131 @@ __device__ __forceinline__ T rescale_factor(T dc, double n) {
   return (m > 0.0 && isfinite(m)) ? (T)(1.0 / m) : (T)1;
 }
 
-// ------------------------------------------------------------------ plane helpers
-// Write u = lw * q (or q when lw is null) into the pair layout of S.
-template <typename T, int NX, int NY>
-__device__ __forceinline__ void load_plane(Cx<T>* S, const T* __restrict__ lw, const T* __restrict__ q) {
-  using C = PlaneCfg<NX, NY>;
-  for (int i = threadIdx.x; i < C::NP; i += blockDim.x) {
-    const int y = i / NX, x = i - y * NX;
-    pair_elem(S, C::KX, y, x) = lw ? lw[i] * q[i] : q[i];
-    if (NY == 1) S[x].y = (T)0;
+// Copy the twiddle tables of this kernel's transform lengths into shared memory (the FFT
+// passes read them every butterfly; shared memory keeps those reads off the L1/L2 path).
+template <typename T, int N>
+__device__ __forceinline__ void stage_twiddles(Cx<T>* dst, const Cx<T>* __restrict__ src) {
+  for (int i = threadIdx.x; i < N; i += blockDim.x) dst[i] = src[i];
+}
+
+// 16-byte vector of T (4 floats or 2 doubles).
+template <typename T>
+struct Vec;
+template <>
+struct Vec<float> {
+  using V = float4;
+  static constexpr int W = 4;
+  __device__ static float get(const float4& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+  __device__ static void set(float4& v, int k, float a) {
+    if (k == 0) v.x = a;
+    else if (k == 1) v.y = a;
+    else if (k == 2) v.z = a;
+    else v.w = a;
+  }
+};
+template <>
+struct Vec<double> {
+  using V = double2;
+  static constexpr int W = 2;
+  __device__ static double get(const double2& v, int k) { return k == 0 ? v.x : v.y; }
+  __device__ static void set(double2& v, int k, double a) {
+    if (k == 0) v.x = a;
+    else v.y = a;
+  }
+};
+
+// Copy n complex values global <-> shared with 16-byte accesses when the byte count allows.
+template <typename T>
+__device__ __forceinline__ void copy_cx(Cx<T>* __restrict__ dst, const Cx<T>* __restrict__ src, int n) {
+  if ((n * sizeof(Cx<T>)) % 16 == 0) {
+    const int nv = (int)(n * sizeof(Cx<T>) / 16);
+    const int4* s4 = reinterpret_cast<const int4*>(src);
+    int4* d4 = reinterpret_cast<int4*>(dst);
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) d4[i] = s4[i];
+  } else {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
   }
 }
 
-// q_out = lw_cur * r (r = plane after the inverse transform); store it, and when lw_next is
-// given put u = lw_next * q_out back into S for the next step.
+// ------------------------------------------------------------------ plane helpers
+// Write u = lw * q (or q when lw is null) into the pair layout of S.  Rows are read with
+// 16-byte vectors (NX is a multiple of the vector width for every supported shape).
+template <typename T, int NX, int NY>
+__device__ __forceinline__ void load_plane(Cx<T>* S, const T* __restrict__ lw, const T* __restrict__ q) {
+  using C = PlaneCfg<NX, NY>;
+  using VT = Vec<T>;
+  using V = typename VT::V;
+  static_assert(NX % VT::W == 0, "row length must be a multiple of the vector width");
+  constexpr int NV = C::NP / VT::W;
+  const V* q4 = reinterpret_cast<const V*>(q);
+  const V* l4 = reinterpret_cast<const V*>(lw);
+  for (int iv = threadIdx.x; iv < NV; iv += blockDim.x) {
+    const int i = iv * VT::W;
+    const int y = i / NX, x = i - y * NX;
+    const V qv = q4[iv];
+    V lv;
+    if (lw) lv = l4[iv];
+#pragma unroll
+    for (int k = 0; k < VT::W; ++k) {
+      const T u = lw ? VT::get(lv, k) * VT::get(qv, k) : VT::get(qv, k);
+      pair_elem(S, C::KX, y, x + k) = u;
+      if (NY == 1) S[x + k].y = (T)0;
+    }
+  }
+}
+
+// q_out = lw_cur * cscale * r (r = plane after the inverse transform); store it, and when
+// lw_next is given put u = lw_next * q_out back into S for the next step.
 template <typename T, int NX, int NY>
 __device__ __forceinline__ void finish_plane(Cx<T>* S, const T* __restrict__ lw_cur, const T* __restrict__ lw_next,
                                              T* __restrict__ qout, T cscale) {
   using C = PlaneCfg<NX, NY>;
-  for (int i = threadIdx.x; i < C::NP; i += blockDim.x) {
+  using VT = Vec<T>;
+  using V = typename VT::V;
+  constexpr int NV = C::NP / VT::W;
+  const V* lc4 = reinterpret_cast<const V*>(lw_cur);
+  const V* ln4 = reinterpret_cast<const V*>(lw_next);
+  V* o4 = reinterpret_cast<V*>(qout);
+  for (int iv = threadIdx.x; iv < NV; iv += blockDim.x) {
+    const int i = iv * VT::W;
     const int y = i / NX, x = i - y * NX;
-    T& e = pair_elem(S, C::KX, y, x);
-    const T qv = lw_cur[i] * (e * cscale);
-    qout[i] = qv;
-    if (lw_next) {
-      e = lw_next[i] * qv;
-      if (NY == 1) S[x].y = (T)0;
+    const V lc = lc4[iv];
+    V ln;
+    if (lw_next) ln = ln4[iv];
+    V ov;
+#pragma unroll
+    for (int k = 0; k < VT::W; ++k) {
+      T& e = pair_elem(S, C::KX, y, x + k);
+      const T qv = VT::get(lc, k) * (e * cscale);
+      VT::set(ov, k, qv);
+      if (lw_next) {
+        e = VT::get(ln, k) * qv;
+        if (NY == 1) S[x + k].y = (T)0;
+      }
     }
+    o4[iv] = ov;
   }
 }
 
 // ------------------------------------------------------------------ Nz == 1 chains
 template <typename T, int NX, int NY>
 __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
-    chain_plane_kernel(const ChainJob<T>* __restrict__ jobs, Twiddles<T> tw) {
+    chain_plane_kernel(const ChainJob<T>* __restrict__ jobs, Twiddles<T> twg) {
   using C = PlaneCfg<NX, NY>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* S = reinterpret_cast<Cx<T>*>(smem_raw);
+  __shared__ Cx<T> twx[NX], twy[NY];
+  stage_twiddles<T, NX>(twx, twg.x);
+  stage_twiddles<T, NY>(twy, twg.y);
+  const Twiddles<T> tw{twx, twy, nullptr};
   const ChainJob<T> job = jobs[blockIdx.x];
 #pragma unroll 1
   for (int t = 0; t < job.nsteps; ++t) {
     const StepOp<T> op = job.ops[t];
     if (t == 0) {
       load_plane<T, NX, NY>(S, op.lw, job.hist + (long)job.s0 * C::NP);
-      __syncthreads();
     }
+    __syncthreads();
     plane_fwd<T, NX, NY>(S, tw.x, tw.y);
     T c = (T)1;
     if (job.csc) {
@@ -172,20 +257,23 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
 
 // ------------------------------------------------------------------ 3D: plane pass
 template <typename T, int NX, int NY>
-__global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
-    xy_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nz, Twiddles<T> tw) {
+__global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, sizeof(T) == 4 ? PlaneCfg<NX, NY>::MINB : 1)
+    xy_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nz, Twiddles<T> twg) {
   using C = PlaneCfg<NX, NY>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* S = reinterpret_cast<Cx<T>*>(smem_raw);
   const ChainJob<T> job = jobs[blockIdx.y];
   if (t > job.nsteps) return;
+  __shared__ Cx<T> twx[NX], twy[NY];
+  stage_twiddles<T, NX>(twx, twg.x);
+  stage_twiddles<T, NY>(twy, twg.y);
+  const Twiddles<T> tw{twx, twy, nullptr};
   const int z = blockIdx.x;
   const long ng = (long)C::NP * nz;
   const bool finish = t >= 1;
   const bool start = t < job.nsteps;
   if (finish) {
-    const Cx<T>* src = job.kbuf + (long)z * C::NKP;
-    for (int k = threadIdx.x; k < C::NKP; k += blockDim.x) S[k] = src[k];
+    copy_cx<T>(S, job.kbuf + (long)z * C::NKP, C::NKP);
     __syncthreads();
     plane_inv<T, NX, NY>(S, tw.x, tw.y);
     const StepOp<T> op = job.ops[t - 1];
@@ -199,36 +287,42 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
   __syncthreads();
   if (start) {
     plane_fwd<T, NX, NY>(S, tw.x, tw.y);
-    Cx<T>* dst = job.kbuf + (long)z * C::NKP;
-    for (int k = threadIdx.x; k < C::NKP; k += blockDim.x) dst[k] = S[k];
+    copy_cx<T>(job.kbuf + (long)z * C::NKP, S, C::NKP);
   }
 }
 
 // ------------------------------------------------------------------ 3D: pencil pass
-// M consecutive pencils (index m = ky*Kx + kx within a plane) of length NZ per CTA.
+// M consecutive pencils (index m = ky*Kx + kx within a plane) of length NZ per CTA.  The tile
+// is pencil-major in shared memory with rows padded by one element, Tl[mm*(NZ+1) + z], so the
+// threads of a transform group read consecutive words and the groups of a warp fall on
+// different banks.
 template <typename T>
 struct ZCfg {
-  static constexpr int M = sizeof(T) == 4 ? 16 : 8;  // 128-byte rows
+  static constexpr int M = sizeof(T) == 4 ? 16 : 8;  // 128-byte rows of the global tile
 };
 
 template <typename T, int NZ>
 __global__ void __launch_bounds__(512)
-    z_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nkp, double ng, Twiddles<T> tw) {
+    z_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nkp, double ng, Twiddles<T> twg) {
   constexpr int M = ZCfg<T>::M;
+  constexpr int LDT = NZ + 1;
   constexpr int TOT = NZ * M;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* Tl = reinterpret_cast<Cx<T>*>(smem_raw);
   const ChainJob<T> job = jobs[blockIdx.y];
   if (t >= job.nsteps) return;
+  __shared__ Cx<T> twz[NZ];
+  stage_twiddles<T, NZ>(twz, twg.z);
+  const Twiddles<T> tw{nullptr, nullptr, twz};
   const int m0 = blockIdx.x * M;
   const int mc = min(M, nkp - m0);
   Cx<T>* kb = job.kbuf;
   for (int i = threadIdx.x; i < TOT; i += blockDim.x) {
     const int zz = i / M, mm = i - zz * M;
-    Tl[i] = (mm < mc) ? kb[(long)zz * nkp + m0 + mm] : cx<T>(0, 0);
+    Tl[mm * LDT + zz] = (mm < mc) ? kb[(long)zz * nkp + m0 + mm] : cx<T>(0, 0);
   }
   __syncthreads();
-  fft_batch_n<T, false, NZ>(Tl, M, 1, M, tw.z);
+  fft_batch_n<T, false, NZ>(Tl, 1, LDT, M, tw.z);
   __syncthreads();
   if (job.csc && blockIdx.x == 0 && threadIdx.x == 0) {
     // the (0, 0, 0) coefficient is the grid sum of LW * q_t
@@ -241,15 +335,16 @@ __global__ void __launch_bounds__(512)
     const int zz = i / M, mm = i - zz * M;
     if (mm < mc) {
       const T f = ld[(long)zz * nkp + m0 + mm];
-      Tl[i] = cx<T>(Tl[i].x * f, Tl[i].y * f);
+      Cx<T>& e = Tl[mm * LDT + zz];
+      e = cx<T>(e.x * f, e.y * f);
     }
   }
   __syncthreads();
-  fft_batch_n<T, true, NZ>(Tl, M, 1, M, tw.z);
+  fft_batch_n<T, true, NZ>(Tl, 1, LDT, M, tw.z);
   __syncthreads();
   for (int i = threadIdx.x; i < TOT; i += blockDim.x) {
     const int zz = i / M, mm = i - zz * M;
-    if (mm < mc) kb[(long)zz * nkp + m0 + mm] = Tl[i];
+    if (mm < mc) kb[(long)zz * nkp + m0 + mm] = Tl[mm * LDT + zz];
   }
 }
 
@@ -260,8 +355,12 @@ __global__ void __launch_bounds__(512)
 template <typename T, int NX, int NY>
 __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
     stress_plane_kernel(const StressItem<T>* __restrict__ items, const double* __restrict__ dksq, int nparams,
-                        double* __restrict__ part, Twiddles<T> tw) {
+                        double* __restrict__ part, Twiddles<T> twg) {
   using C = PlaneCfg<NX, NY>;
+  __shared__ Cx<T> twx[NX], twy[NY];
+  stage_twiddles<T, NX>(twx, twg.x);
+  stage_twiddles<T, NY>(twy, twg.y);
+  const Twiddles<T> tw{twx, twy, nullptr};
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* S = reinterpret_cast<Cx<T>*>(smem_raw);
   T* req = reinterpret_cast<T*>(S + C::SLOTS);
@@ -291,8 +390,12 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
 // half-spectrum buffers dst[item] (one CTA per (z, item)).
 template <typename T, int NX, int NY>
 __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
-    xy_fwd_kernel(const T* const* __restrict__ src, Cx<T>* const* __restrict__ dst, Twiddles<T> tw) {
+    xy_fwd_kernel(const T* const* __restrict__ src, Cx<T>* const* __restrict__ dst, Twiddles<T> twg) {
   using C = PlaneCfg<NX, NY>;
+  __shared__ Cx<T> twx[NX], twy[NY];
+  stage_twiddles<T, NX>(twx, twg.x);
+  stage_twiddles<T, NY>(twy, twg.y);
+  const Twiddles<T> tw{twx, twy, nullptr};
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* S = reinterpret_cast<Cx<T>*>(smem_raw);
   const int z = blockIdx.x;
@@ -308,12 +411,16 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
 template <typename T, int NZ>
 __global__ void __launch_bounds__(512)
     z_fwd_stress_kernel(Cx<T>* const* __restrict__ kq, Cx<T>* const* __restrict__ kqc, int nkp,
-                        const double* __restrict__ dksq, int nparams, double* __restrict__ part, Twiddles<T> tw) {
+                        const double* __restrict__ dksq, int nparams, double* __restrict__ part, Twiddles<T> twg) {
   constexpr int M = ZCfg<T>::M;
+  constexpr int LDT = NZ + 1;
+  __shared__ Cx<T> twz[NZ];
+  stage_twiddles<T, NZ>(twz, twg.z);
+  const Twiddles<T> tw{nullptr, nullptr, twz};
   constexpr int TOT = NZ * M;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* A = reinterpret_cast<Cx<T>*>(smem_raw);
-  Cx<T>* B = A + TOT;
+  Cx<T>* B = A + M * LDT;
   __shared__ double red[kMaxParams][32];
   const long nk = (long)nkp * NZ;
   const int m0 = blockIdx.x * M;
@@ -322,12 +429,12 @@ __global__ void __launch_bounds__(512)
   const Cx<T>* b = kqc[blockIdx.y];
   for (int i = threadIdx.x; i < TOT; i += blockDim.x) {
     const int zz = i / M, mm = i - zz * M;
-    A[i] = (mm < mc) ? a[(long)zz * nkp + m0 + mm] : cx<T>(0, 0);
-    B[i] = (mm < mc) ? b[(long)zz * nkp + m0 + mm] : cx<T>(0, 0);
+    A[mm * LDT + zz] = (mm < mc) ? a[(long)zz * nkp + m0 + mm] : cx<T>(0, 0);
+    B[mm * LDT + zz] = (mm < mc) ? b[(long)zz * nkp + m0 + mm] : cx<T>(0, 0);
   }
   __syncthreads();
-  fft_batch_n<T, false, NZ>(A, M, 1, M, tw.z);
-  fft_batch_n<T, false, NZ>(B, M, 1, M, tw.z);
+  fft_batch_n<T, false, NZ>(A, 1, LDT, M, tw.z);
+  fft_batch_n<T, false, NZ>(B, 1, LDT, M, tw.z);
   __syncthreads();
   double acc[kMaxParams];
   for (int p = 0; p < kMaxParams; ++p) acc[p] = 0.0;
@@ -335,7 +442,7 @@ __global__ void __launch_bounds__(512)
     const int zz = i / M, mm = i - zz * M;
     if (mm < mc) {
       const long k = (long)zz * nkp + m0 + mm;
-      const double prod = (double)A[i].x * (double)B[i].x * (k == 0 ? 1.0 : 2.0);
+      const double prod = (double)A[mm * LDT + zz].x * (double)B[mm * LDT + zz].x * (k == 0 ? 1.0 : 2.0);
       for (int p = 0; p < nparams; ++p) acc[p] += prod * dksq[p * nk + k];
     }
   }
@@ -358,23 +465,24 @@ static constexpr size_t plane_smem() {
 
 static inline int shape_key(int nx, int ny) { return nx * 1024 + ny; }
 
-template <typename T>
-static int z_threads() {
-  return 256;
+template <typename T, int NZ>
+static constexpr int z_threads() {
+  constexpr int t = ZCfg<T>::M * Plan<NZ>::G;
+  return t < 64 ? 64 : t;
 }
 
 template <typename T, int NZ>
 static void launch_z_step(const ChainJob<T>* jobs, int t, int nkp, double ng, int njobs, const Twiddles<T>& tw,
                           cudaStream_t st) {
   constexpr int M = ZCfg<T>::M;
-  const size_t sz = sizeof(Cx<T>) * (size_t)NZ * M;
+  const size_t sz = sizeof(Cx<T>) * (size_t)(NZ + 1) * M;
   static bool attr = false;
   if (!attr) {
     set_smem(z_step_kernel<T, NZ>, sz);
     attr = true;
   }
   const int ntiles = (nkp + M - 1) / M;
-  z_step_kernel<T, NZ><<<dim3(ntiles, njobs), z_threads<T>(), sz, st>>>(jobs, t, nkp, ng, tw);
+  z_step_kernel<T, NZ><<<dim3(ntiles, njobs), z_threads<T, NZ>(), sz, st>>>(jobs, t, nkp, ng, tw);
     count_launches(1);
 }
 
@@ -444,13 +552,13 @@ static void stress_shape(const StressItem<T>* items, int nitems, const T* const*
   switch (nz) {
 #define PF_Z(N)                                                                                              \
   case N: {                                                                                                  \
-    const size_t sz = 2 * sizeof(Cx<T>) * (size_t)N * M;                                                     \
+    const size_t sz = 2 * sizeof(Cx<T>) * (size_t)(N + 1) * M;                                               \
     static bool za = false;                                                                                  \
     if (!za) {                                                                                               \
       set_smem(z_fwd_stress_kernel<T, N>, sz);                                                               \
       za = true;                                                                                             \
     }                                                                                                        \
-    z_fwd_stress_kernel<T, N><<<dim3(ntiles, nitems), 256, sz, st>>>(kq, kqc, C::NKP, dksq, nparams, part, tw); count_launches(1); \
+    z_fwd_stress_kernel<T, N><<<dim3(ntiles, nitems), z_threads<T, N>(), sz, st>>>(kq, kqc, C::NKP, dksq, nparams, part, tw); count_launches(1); \
   } break;
     PF_Z_LENGTHS(PF_Z)
 #undef PF_Z

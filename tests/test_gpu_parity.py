@@ -230,7 +230,7 @@ def test_fp32_rescaled_strong_fields():
         assert g.species[isp].Q == pytest.approx(o.species[isp].Q, rel=FP32_RTOL)
     for mid in (1, 2):
         assert rel(g.density[mid], o.density[mid]) < 2 * FP32_RTOL
-    assert g.free_energy() == pytest.approx(o.free_energy(), rel=1e-5)
+    assert g.free_energy() == pytest.approx(o.free_energy(), rel=1e-4)
     assert np.allclose(g.scfstress(), o.scfstress(), rtol=2e-3, atol=1e-9)
 
 
