@@ -33,7 +33,8 @@ enum pf_status {
   PF_ETIMEOUT = 5,    /* a bounded device wait gave up */
   PF_ESTATE = 6,      /* call out of order (e.g. step before setup) */
   PF_ENOMEM = 7,      /* device allocation failed */
-  PF_EUNSUPPORTED = 8 /* grid length outside the supported FFT sizes */
+  PF_EUNSUPPORTED = 8, /* grid length outside the supported FFT sizes */
+  PF_ETOOLARGE = 9     /* pf_propagate_noalloc: the grid does not fit its fixed scratch array */
 };
 
 enum pf_precision {
@@ -149,6 +150,23 @@ int pf_scft(pf_system* sys, const pf_scft_options* opts, int use_domain, pf_scft
  * handle's current cell; qout receives the last step.  Host arrays. */
 int pf_propagate(pf_system* sys, const double* omega, double vol, double b, double ds,
                  const double* qin, double* qout, int nsteps);
+
+/* ---- allocation-free propagation (no counterpart in the reference) ----
+ * For callers that cannot allocate device memory (code inside another framework's memory
+ * pool, allocation-free real-time paths, bindings that own every device buffer): runs nsteps
+ * RK2 contour steps of one chain entirely on caller-provided device buffers and calls no
+ * cudaMalloc/cudaFree.  hist holds (nsteps+1) grids of Nx*Ny*Nz values of the precision's
+ * type (float64 for PF_FP64, float32 for PF_FP32): grid 0 is the input q, grids 1..nsteps
+ * receive the steps.  lw is the Nx*Ny*Nz real-space factor exp(-ds*vol*w/2); ld is the half
+ * spectrum factor exp(-ds*b^2*|k|^2/6)/(Nx*Ny*Nz), (Nx/2+1)*Ny*Nz values, layout [kz][ky][kx].
+ * Work is queued on `stream` (a cudaStream_t; NULL = default stream) and is complete when
+ * that stream is.  Internal state lives in one 16 MiB __device__ array per GPU (held until
+ * the process exits): the 3D half spectrum must fit 16 MiB - 80 KiB (float32 up to 128^3,
+ * float64 up to 96^3), otherwise PF_ETOOLARGE; nsteps <= 3840.  Calls whose GPU work
+ * overlaps race on that array.  The first call on each device looks up the array's device
+ * address, so make it before any stream capture. */
+int pf_propagate_noalloc(int nx, int ny, int nz, int precision, void* hist, const void* lw, const void* ld,
+                         int nsteps, void* stream);
 
 /* ---- measurement ---- */
 /* Device time (ms) of the last density solve's propagator launches, measured with CUDA

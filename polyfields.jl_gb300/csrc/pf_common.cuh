@@ -49,6 +49,7 @@ enum Status : int {
   E_STATE = 6,
   E_NOMEM = 7,
   E_UNSUPPORTED = 8,
+  E_TOOLARGE = 9,
 };
 
 // Transform lengths along one axis supported by the in-shared-memory FFTs.

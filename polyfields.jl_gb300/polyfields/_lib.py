@@ -11,7 +11,8 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libpolyfields_gpu.so")
 
-PF_OK, PF_EARG, PF_ECUDA, PF_ENAN, PF_ESINGULAR, PF_ETIMEOUT, PF_ESTATE, PF_ENOMEM, PF_EUNSUPPORTED = range(9)
+(PF_OK, PF_EARG, PF_ECUDA, PF_ENAN, PF_ESINGULAR, PF_ETIMEOUT, PF_ESTATE, PF_ENOMEM, PF_EUNSUPPORTED,
+ PF_ETOOLARGE) = range(10)
 PF_FP64, PF_FP32 = 0, 1
 PF_FIELD, PF_DENSITY, PF_RESIDUAL, PF_POTENTIAL = range(4)
 
@@ -67,6 +68,7 @@ SIGNATURES = {
     "pf_domain_stress_error": (_c_int, [_vp, _dptr]),
     "pf_scft": (_c_int, [_vp, ctypes.POINTER(ScftOptions), _c_int, ctypes.POINTER(ScftResults)]),
     "pf_propagate": (_c_int, [_vp, _dptr, _c_double, _c_double, _c_double, _dptr, _dptr, _c_int]),
+    "pf_propagate_noalloc": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _c_int, _vp]),
     "pf_set_timing": (_c_int, [_vp, _c_int]),
     "pf_last_timing": (_c_int, [_vp, _dptr, _dptr, _iptr]),
     "pf_record_event": (_c_int, [_vp, _c_int]),
