@@ -158,10 +158,11 @@ int pf_propagate(pf_system* sys, const double* omega, double vol, double b, doub
  * cudaMalloc/cudaFree.  hist holds (nsteps+1) grids of Nx*Ny*Nz values of the precision's
  * type (float64 for PF_FP64, float32 for PF_FP32): grid 0 is the input q, grids 1..nsteps
  * receive the steps.  lw is the Nx*Ny*Nz real-space factor exp(-ds*vol*w/2); ld is the half
- * spectrum factor exp(-ds*b^2*|k|^2/6)/(Nx*Ny*Nz), (Nx/2+1)*Ny*Nz values, layout [kz][ky][kx].
+ * spectrum factor exp(-ds*b^2*|k|^2/6)/(Nx*Ny*Nz), (Nx/2+1)*Ny*Nz values, layout [kz][kx][ky]
+ * (ky fastest).
  * Work is queued on `stream` (a cudaStream_t; NULL = default stream) and is complete when
  * that stream is.  Internal state lives in one 16 MiB __device__ array per GPU (held until
- * the process exits): the 3D half spectrum must fit 16 MiB - 80 KiB (float32 up to 128^3,
+ * the process exits): the 3D half spectrum must fit 16 MiB - 96 KiB (float32 up to 128^3,
  * float64 up to 96^3), otherwise PF_ETOOLARGE; nsteps <= 3840.  Calls whose GPU work
  * overlaps race on that array.  The first call on each device looks up the array's device
  * address, so make it before any stream capture. */

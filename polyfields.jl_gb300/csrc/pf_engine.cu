@@ -391,6 +391,7 @@ struct System {
   DevBuf w, pot, res, rho;   // nmon * ng doubles
   DevBuf part, sums, stats4, packed, cn, status;
   DevBuf twid[2];
+  int tw_off[2][3] = {};  // offsets of the x, y, z tables in twid
   DevBuf dksq;
   DevBuf jobs[2];
   int njobs = 0, maxsteps = 0;
@@ -465,20 +466,20 @@ struct System {
     const int lens[3] = {nx, ny, nz};
     std::vector<Cx<T>> h;
     for (int a = 0; a < 3; ++a) {
-      const int n = lens[a];
-      for (int m = 0; m < n; ++m) {
-        // exp(-2 pi i m / n) with the angle reduced to the first octant for accuracy
-        const long double ang = -2.0L * 3.141592653589793238462643383279502884L * (long double)m / (long double)n;
-        h.push_back(cx<T>((T)std::cos(ang), (T)std::sin(ang)));
-      }
+      tw_off[p][a] = (int)h.size();
+      std::vector<double> re(2048), im(2048);
+      const int cnt = fft_twiddle_table(lens[a], re.data(), im.data(), 2048);
+      if (cnt < 0) throw PFError(E_UNSUPPORTED, "no FFT plan for length " + std::to_string(lens[a]));
+      for (int i = 0; i < cnt; ++i) h.push_back(cx<T>((T)re[i], (T)im[i]));
     }
+    if (h.empty()) h.push_back(cx<T>(1, 0));
     twid[p].alloc(sizeof(Cx<T>) * h.size());
     PF_CU(cudaMemcpy(twid[p].p, h.data(), sizeof(Cx<T>) * h.size(), cudaMemcpyHostToDevice));
   }
   template <typename T>
   Twiddles<T> tw(int p) const {
     const Cx<T>* b = twid[p].as<Cx<T>>();
-    return Twiddles<T>{b, b + nx, b + nx + ny};
+    return Twiddles<T>{b + tw_off[p][0], b + tw_off[p][1], b + tw_off[p][2]};
   }
 
   CellGeom geom() const {

@@ -77,6 +77,10 @@ long launch_total();
 template <typename T>
 constexpr int z_tile_pencils() { return sizeof(T) == 4 ? 16 : 8; }
 template <typename T> bool shape_supported(int nx, int ny, int nz);
+// Twiddle tables of one transform length for the in-kernel FFTs: the per-pass tables of the
+// plan in A order followed by those in B order, forward sign, written as (re[i], im[i]).
+// Returns the number of entries (0 for n = 1, -1 for an unsupported length or short buffers).
+int fft_twiddle_table(int n, double* re, double* im, int max_entries);
 template <typename T> void launch_lw(T* lw, const double* w, double coeff, long n, cudaStream_t st);
 template <typename T> void launch_ld(T* ld, const CellGeom& g, double coeff, double scale, long nk, cudaStream_t st);
 void launch_dksq(double* dk, const CellGeom& g, int nparams, long nk, cudaStream_t st);

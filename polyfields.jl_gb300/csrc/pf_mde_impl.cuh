@@ -6,15 +6,22 @@
 // spectrum (the 1/Ng of the normalised irfft folded in).
 //
 // Layout in HBM: a real grid is Nz planes of Ny rows of Nx values, x fastest (the
-// reference's column-major Array{Float64,3}[x,y,z]); the half spectrum is Nz planes of
-// Ny rows of Kx = Nx/2+1 complex values.  A propagator history is (Ns+1) consecutive grids.
+// reference's column-major Array{Float64,3}[x,y,z]).  Half-spectrum arrays of the engine
+// (LD, dksq, the 3D scratch) are Nz planes of Kx = Nx/2+1 columns of Ny values, ky fastest:
+// [kz][kx][ky].  A propagator history is (Ns+1) consecutive grids.
 //
-// Grids with Nz == 1 (1D and 2D systems) hold a whole plane in one CTA's shared memory,
-// so one persistent CTA runs all contour steps of a chain (chain_plane_kernel).  3D grids
-// split each step into a plane pass (x and y transforms, one CTA per z plane:
-// xy_step_kernel) and a pencil pass (z transforms and LD, one CTA per tile of pencils:
-// z_step_kernel); the plane pass of step t fuses the end of step t-1 (inverse transforms,
-// LW, store q) with the start of step t (LW, forward transforms).  Independent chains
+// A plane (one z slice) is transformed by one CTA: the real rows 2p, 2p+1 ride one complex
+// FFT along x (two-for-one), the Kx columns are transformed along y.  Row pairs and columns
+// share one shared-memory buffer S of Kx * max(Ny, 2) complex values: pair p owns the span
+// S[2p Kx, 2p Kx + 2 Kx) and column kx the strided elements S[y Kx + kx].  Transform passes
+// read and write global memory directly where they can (first y-inverse pass, last
+// y-forward pass, first and last z pass), and the x-inverse -> LW -> store q -> LW ->
+// x-forward sequence and the LD multiplies happen in registers between two passes.
+//
+// Grids with Nz == 1 (1D and 2D systems): one persistent CTA per chain runs all contour
+// steps (chain_plane_kernel).  3D grids: each step is a plane pass (xy_step_kernel, one CTA
+// per z plane) and a pencil pass (z_step_kernel, one CTA per 16 or 8 pencils); the plane
+// pass of step t fuses the end of step t-1 with the start of step t.  Independent chains
 // (forward q, backward qc, other species) advance together in the same launches.
 //
 // Every kernel is specialised on its transform lengths at compile time; the host picks the
@@ -31,16 +38,46 @@ namespace pf {
   X(48, 48) X(64, 64) X(96, 96) X(128, 128) X(32, 16) X(64, 32) X(96, 48) X(128, 64)
 #define PF_Z_LENGTHS(X) X(8) X(16) X(32) X(48) X(64) X(96) X(128) X(256)
 
+__host__ __device__ constexpr int round32(int n) { return (n + 31) / 32 * 32; }
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+
+// twiddle entries of both orders of a length (1 for a length-1 axis, which has no transform)
+template <int N>
+__host__ __device__ constexpr int tw_total() {
+  if constexpr (N > 1) return Order<N, 0>::TW_SIZE + Order<N, 1>::TW_SIZE;
+  else return 1;
+}
+template <int N>
+__host__ __device__ constexpr int plan_group() {
+  if constexpr (N > 1) return Plan<N>::G;
+  else return 1;
+}
+
 template <int NX, int NY>
 struct PlaneCfg {
   static constexpr int KX = NX / 2 + 1;
-  static constexpr int NKP = KX * NY;                 // half-spectrum points of a plane
-  static constexpr int NP = NX * NY;                  // real points of a plane
-  static constexpr int SLOTS = KX * (NY > 1 ? NY : 2);  // complex slots of the work plane
-  static constexpr int THREADS = NY == 1 ? 32 : (NKP >= 4096 ? 512 : (NKP >= 1024 ? 256 : 128));
-  // float32 planes of >= 4096 spectral points: two CTAs per SM fit the shared memory, so ask
-  // the register allocator for that occupancy
-  static constexpr int MINB = NKP >= 4096 ? 2 : 1;
+  static constexpr int NKP = KX * NY;                    // half-spectrum points of a plane
+  static constexpr int NP = NX * NY;                     // real points of a plane
+  static constexpr int SLOTS = KX * (NY > 1 ? NY : 2);   // complex slots of S
+  static constexpr int NPAIR = NY > 1 ? NY / 2 : 1;
+  static constexpr int GX = Plan<NX>::G;
+  static constexpr int GY = plan_group<NY>();
+  static constexpr int SP = pair_stride<NX>();
+  static constexpr int SC = NY > 1 ? col_stride<NY>() : 1;
+  // one group per row pair and one per column, all in one round
+  static constexpr int THREADS =
+      32 * cmax(warps_for<GX, SP>(NPAIR), NY > 1 ? warps_for<(NY > 1 ? plan_group<NY>() : 32), SC>(KX) : 1);
+  static constexpr int TWX = tw_total<NX>();
+  static constexpr int TWY = tw_total<NY>();
+  // the whole register file for one CTA (persistent chain kernels run one CTA per SM): each of
+  // the SM's four sub-partitions holds 16384 registers for ceil(warps / 4) of the CTA's warps
+  static constexpr int WPS = (THREADS / 32 + 3) / 4;
+  static constexpr int MAXREG = (16384 / (WPS * 32) / 8 * 8) > 255 ? 255 : (16384 / (WPS * 32) / 8 * 8);
+};
+
+template <typename T>
+struct ZCfg {
+  static constexpr int M = sizeof(T) == 4 ? 16 : 8;  // pencils per tile (128-byte rows)
 };
 
 // ------------------------------------------------------------------ operator setup
@@ -64,26 +101,31 @@ __device__ __forceinline__ double ksq_at(const CellGeom& g, int ix, int iy, int 
   return kx * kx + ky * ky + kz * kz;
 }
 
+// (ix, iy, iz) of half-spectrum index i in the [kz][kx][ky] layout
+__device__ __forceinline__ void spectral_index(const CellGeom& g, long i, int& ix, int& iy, int& iz) {
+  const long nkp = (long)(g.nx / 2 + 1) * g.ny;
+  iz = (int)(i / nkp);
+  const long r = i - (long)iz * nkp;
+  ix = (int)(r / g.ny);
+  iy = (int)(r - (long)ix * g.ny);
+}
+
 template <typename T>
 __global__ void ld_kernel(T* __restrict__ ld, CellGeom g, double coeff, double scale) {
-  const int kxn = g.nx / 2 + 1;
-  const long nk = (long)kxn * g.ny * g.nz;
+  const long nk = (long)(g.nx / 2 + 1) * g.ny * g.nz;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nk; i += (long)gridDim.x * blockDim.x) {
-    const int ix = (int)(i % kxn);
-    const int iy = (int)((i / kxn) % g.ny);
-    const int iz = (int)(i / ((long)kxn * g.ny));
+    int ix, iy, iz;
+    spectral_index(g, i, ix, iy, iz);
     ld[i] = (T)(exp(-coeff * ksq_at(g, ix, iy, iz)) * scale);
   }
 }
 
 // dksq for every cell parameter (src/system/cell.jl:292-320), nparams grids of Nk.
 static __global__ void dksq_kernel(double* __restrict__ dk, CellGeom g, int nparams) {
-  const int kxn = g.nx / 2 + 1;
-  const long nk = (long)kxn * g.ny * g.nz;
+  const long nk = (long)(g.nx / 2 + 1) * g.ny * g.nz;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nk; i += (long)gridDim.x * blockDim.x) {
-    const int ix = (int)(i % kxn);
-    const int iy = (int)((i / kxn) % g.ny);
-    const int iz = (int)(i / ((long)kxn * g.ny));
+    int ix, iy, iz;
+    spectral_index(g, i, ix, iy, iz);
     const double j[3] = {(double)ix, fold_index(iy, g.ny), fold_index(iz, g.nz)};
     for (int p = 0; p < nparams; ++p) {
       double acc = 0.0;
@@ -107,348 +149,684 @@ __device__ __forceinline__ T rescale_factor(T dc, double n) {
   return (m > 0.0 && isfinite(m)) ? (T)(1.0 / m) : (T)1;
 }
 
-// Copy the twiddle tables of this kernel's transform lengths into shared memory (the FFT
-// passes read them every butterfly; shared memory keeps those reads off the L1/L2 path).
+template <typename T>
+__device__ __forceinline__ void stage(Cx<T>* dst, const Cx<T>* __restrict__ src, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+// ------------------------------------------------------------------ plane pipeline pieces
+// Registers at the x join: z(x) = (row 2p, row 2p+1) at positions Join<NX>::pos.
+template <typename T, int NX>
+struct XRegs {
+  Cx<T> v[Join<NX>::BPT][Join<NX>::R];
+};
+// Registers at the y (or z) forward -> inverse join: positions JoinBA<N>::pos.
 template <typename T, int N>
-__device__ __forceinline__ void stage_twiddles(Cx<T>* dst, const Cx<T>* __restrict__ src) {
-  for (int i = threadIdx.x; i < N; i += blockDim.x) dst[i] = src[i];
-}
-
-// 16-byte vector of T (4 floats or 2 doubles).
-template <typename T>
-struct Vec;
-template <>
-struct Vec<float> {
-  using V = float4;
-  static constexpr int W = 4;
-  __device__ static float get(const float4& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
-  __device__ static void set(float4& v, int k, float a) {
-    if (k == 0) v.x = a;
-    else if (k == 1) v.y = a;
-    else if (k == 2) v.z = a;
-    else v.w = a;
-  }
-};
-template <>
-struct Vec<double> {
-  using V = double2;
-  static constexpr int W = 2;
-  __device__ static double get(const double2& v, int k) { return k == 0 ? v.x : v.y; }
-  __device__ static void set(double2& v, int k, double a) {
-    if (k == 0) v.x = a;
-    else v.y = a;
-  }
+struct BARegs {
+  Cx<T> v[JoinBA<N>::BPT][JoinBA<N>::R];
 };
 
-// Copy n complex values global <-> shared with 16-byte accesses when the byte count allows.
-template <typename T>
-__device__ __forceinline__ void copy_cx(Cx<T>* __restrict__ dst, const Cx<T>* __restrict__ src, int n) {
-  if ((n * sizeof(Cx<T>)) % 16 == 0) {
-    const int nv = (int)(n * sizeof(Cx<T>) / 16);
-    const int4* s4 = reinterpret_cast<const int4*>(src);
-    int4* d4 = reinterpret_cast<int4*>(dst);
-    for (int i = threadIdx.x; i < nv; i += blockDim.x) d4[i] = s4[i];
-  } else {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
-  }
-}
-
-// ------------------------------------------------------------------ plane helpers
-// Write u = lw * q (or q when lw is null) into the pair layout of S.  Rows are read with
-// 16-byte vectors (NX is a multiple of the vector width for every supported shape).
+// Column transforms, inverse, order A: from the [kx][ky] global plane kin into
+// S[y Kx + kx].  Group c < Kx handles column c.  The caller syncs the CTA afterwards.
 template <typename T, int NX, int NY>
-__device__ __forceinline__ void load_plane(Cx<T>* S, const T* __restrict__ lw, const T* __restrict__ q) {
+__device__ __forceinline__ void y_inverse_from_global(Cx<T>* S, const Cx<T>* __restrict__ kin, const Cx<T>* twy) {
   using C = PlaneCfg<NX, NY>;
-  using VT = Vec<T>;
-  using V = typename VT::V;
-  static_assert(NX % VT::W == 0, "row length must be a multiple of the vector width");
-  constexpr int NV = C::NP / VT::W;
-  const V* q4 = reinterpret_cast<const V*>(q);
-  const V* l4 = reinterpret_cast<const V*>(lw);
-  for (int iv = threadIdx.x; iv < NV; iv += blockDim.x) {
-    const int i = iv * VT::W;
-    const int y = i / NX, x = i - y * NX;
-    const V qv = q4[iv];
-    V lv;
-    if (lw) lv = l4[iv];
-#pragma unroll
-    for (int k = 0; k < VT::W; ++k) {
-      const T u = lw ? VT::get(lv, k) * VT::get(qv, k) : VT::get(qv, k);
-      pair_elem(S, C::KX, y, x + k) = u;
-      if (NY == 1) S[x + k].y = (T)0;
+  constexpr int P = Order<NY, 0>::P;
+  const int c = group_index<C::GY, C::SC>(threadIdx.x / C::GY), g = threadIdx.x % C::GY;
+  const bool active = c < C::KX;
+  Cx<T>* col = S + (active ? c : 0);
+  using P0 = PassOf<T, true, NY, 0, 0>;
+  Cx<T> v[P0::BPT][Order<NY, 0>::radix(0)];
+  if (active) {
+    P0::load(v, g, [&](int i) { return kin[c * NY + i]; });
+    P0::compute(v, g, twy);
+    P0::store(v, g, [&](int i, const Cx<T>& x) { col[(P > 1 ? swz(i) : i) * C::KX] = x; });
+  }
+  __syncwarp();
+  smem_passes<T, true, NY, 0, 1, P, true, false>(col, C::KX, g, twy, active);
+}
+
+// Column transforms, inverse, order A, starting from registers at the forward -> inverse join
+// (after the LD multiply) and ending in S[y Kx + c].  The caller syncs the CTA afterwards.
+template <typename T, int NX, int NY>
+__device__ __forceinline__ void y_inverse_from_regs(Cx<T>* S, const Cx<T>* twy, BARegs<T, NY>& w, int c, int g,
+                                                    bool active) {
+  using C = PlaneCfg<NX, NY>;
+  constexpr int P = Order<NY, 0>::P;
+  Cx<T>* col = S + (active ? c : 0);
+  using P0 = PassOf<T, true, NY, 0, 0>;
+  if (active) {
+    P0::compute(w.v, g, twy);
+    P0::store(w.v, g, [&](int i, const Cx<T>& x) { col[(P > 1 ? swz(i) : i) * C::KX] = x; });
+  }
+  __syncwarp();
+  smem_passes<T, true, NY, 0, 1, P, true, false>(col, C::KX, g, twy, active);
+}
+
+// Row-pair transforms, inverse, order A: the half spectra of rows 2p, 2p+1 in S -> registers at
+// the x join.  The first pass builds z(x) = A(x) + i B(x) from the Hermitian halves.  Needs the
+// CTA synced before (S written by the column transforms).
+template <typename T, int NX, int NY>
+__device__ __forceinline__ void x_inverse_to_regs(Cx<T>* S, const Cx<T>* twx, XRegs<T, NX>& out, int p, int g,
+                                                  bool active) {
+  using C = PlaneCfg<NX, NY>;
+  constexpr int P = Order<NX, 0>::P;
+  Cx<T>* z = S + (active ? p : 0) * 2 * C::KX;
+  auto build = [&](int x) {
+    Cx<T> A, B;
+    if (x <= NX / 2) {
+      A = z[x];
+      B = NY > 1 ? z[C::KX + x] : cx<T>(0, 0);
+    } else {
+      A = conj(z[NX - x]);
+      B = NY > 1 ? conj(z[C::KX + NX - x]) : cx<T>(0, 0);
     }
+    return cx<T>(A.x - B.y, A.y + B.x);
+  };
+  using P0 = PassOf<T, true, NX, 0, 0>;
+  if constexpr (P == 1) {
+    if (active) {
+      P0::load(out.v, g, build);
+      P0::compute(out.v, g, twx);
+    }
+    __syncwarp();
+  } else {
+    Cx<T> v[P0::BPT][Order<NX, 0>::radix(0)];
+    if (active) {
+      P0::load(v, g, build);
+      P0::compute(v, g, twx);
+    }
+    __syncwarp();
+    if (active) P0::store(v, g, [&](int i, const Cx<T>& x) { z[swz(i)] = x; });
+    __syncwarp();
+    smem_passes<T, true, NX, 0, 1, P - 1, true, true>(z, 1, g, twx, active);
+    using PL = PassOf<T, true, NX, 0, P - 1>;
+    if (active) {
+      PL::load(out.v, g, [&](int i) { return z[swz(i)]; });
+      PL::compute(out.v, g, twx + Order<NX, 0>::tw_offset(P - 1));
+    }
+    __syncwarp();
   }
 }
 
-// q_out = lw_cur * cscale * r (r = plane after the inverse transform); store it, and when
-// lw_next is given put u = lw_next * q_out back into S for the next step.
+// Row-pair transforms, forward, order B: registers at the x join -> z(x) in the pair's span of S
+// (natural order).  The caller syncs the CTA afterwards.
 template <typename T, int NX, int NY>
-__device__ __forceinline__ void finish_plane(Cx<T>* S, const T* __restrict__ lw_cur, const T* __restrict__ lw_next,
-                                             T* __restrict__ qout, T cscale) {
+__device__ __forceinline__ void x_forward_from_regs(Cx<T>* S, const Cx<T>* twx, XRegs<T, NX>& in, int p, int g,
+                                                    bool active) {
   using C = PlaneCfg<NX, NY>;
-  using VT = Vec<T>;
-  using V = typename VT::V;
-  constexpr int NV = C::NP / VT::W;
-  const V* lc4 = reinterpret_cast<const V*>(lw_cur);
-  const V* ln4 = reinterpret_cast<const V*>(lw_next);
-  V* o4 = reinterpret_cast<V*>(qout);
-  for (int iv = threadIdx.x; iv < NV; iv += blockDim.x) {
-    const int i = iv * VT::W;
-    const int y = i / NX, x = i - y * NX;
-    const V lc = lc4[iv];
-    V ln;
-    if (lw_next) ln = ln4[iv];
-    V ov;
+  constexpr int P = Order<NX, 1>::P;
+  Cx<T>* z = S + (active ? p : 0) * 2 * C::KX;
+  const Cx<T>* twb = twx + Order<NX, 0>::TW_SIZE;
+  using P0 = PassOf<T, false, NX, 1, 0>;
+  if (active) {
+    P0::compute(in.v, g, twb);
+    P0::store(in.v, g, [&](int i, const Cx<T>& x) { z[P > 1 ? swz(i) : i] = x; });
+  }
+  __syncwarp();
+  smem_passes<T, false, NX, 1, 1, P, true, false>(z, 1, g, twb, active);
+}
+
+// Column transforms, forward, order B, ending in registers (positions JoinBA<NY>::pos of column
+// c).  The first pass unpacks the row pairs' spectra, A = (Z_k + conj Z_{N-k})/2 (row 2p) and
+// B = (Z_k - conj Z_{N-k})/(2i) (row 2p+1); a CTA-wide barrier separates its reads of every
+// pair span from its writes (all columns are handled in one round).  Needs the CTA synced
+// before (S written by the row transforms).
+template <typename T, int NX, int NY>
+__device__ __forceinline__ void y_forward_to_regs(Cx<T>* S, const Cx<T>* twy, BARegs<T, NY>& out, int c, int g,
+                                                  bool active) {
+  using C = PlaneCfg<NX, NY>;
+  constexpr int P = Order<NY, 1>::P;
+  const Cx<T>* twb = twy + Order<NY, 0>::TW_SIZE;
+  auto unpack = [&](int y) {
+    const Cx<T>* z = S + (y >> 1) * 2 * C::KX;
+    const Cx<T> zk = z[c];
+    const Cx<T> zn = z[(NX - c) % NX];
+    return (y & 1) ? cx<T>((T)0.5 * (zk.y + zn.y), (T)0.5 * (zn.x - zk.x))
+                   : cx<T>((T)0.5 * (zk.x + zn.x), (T)0.5 * (zk.y - zn.y));
+  };
+  using P0 = PassOf<T, false, NY, 1, 0>;
+  if constexpr (P == 1) {
+    if (active) {
+      P0::load(out.v, g, unpack);
+      P0::compute(out.v, g, twb);
+    }
+    __syncthreads();
+  } else {
+    Cx<T> v[P0::BPT][Order<NY, 1>::radix(0)];
+    if (active) {
+      P0::load(v, g, unpack);
+      P0::compute(v, g, twb);
+    }
+    __syncthreads();
+    Cx<T>* col = S + (active ? c : 0);
+    if (active) P0::store(v, g, [&](int i, const Cx<T>& x) { col[swz(i) * C::KX] = x; });
+    __syncwarp();
+    smem_passes<T, false, NY, 1, 1, P - 1, true, true>(col, C::KX, g, twb, active);
+    using PL = PassOf<T, false, NY, 1, P - 1>;
+    if (active) {
+      PL::load(out.v, g, [&](int i) { return col[swz(i) * C::KX]; });
+      PL::compute(out.v, g, twb + Order<NY, 1>::tw_offset(P - 1));
+    }
+    __syncwarp();
+  }
+}
+
+// Finish step t-1 and start step t on the registers of one row pair:
+// q = lw_cur * (cs * r) is stored; u = lw_next * q goes back into the registers.  Inside a
+// block lw_next is lw_cur (the same array), which is then read once.
+template <typename T, int NX, int NY>
+__device__ __forceinline__ void finish_regs(XRegs<T, NX>& r, int p, int g, const T* __restrict__ lw_cur,
+                                            const T* __restrict__ lw_next, T* __restrict__ qout, T cs) {
+  using J = Join<NX>;
+  const int y0 = 2 * p, y1 = 2 * p + 1;
+  const bool same = lw_next == lw_cur;
 #pragma unroll
-    for (int k = 0; k < VT::W; ++k) {
-      T& e = pair_elem(S, C::KX, y, x + k);
-      const T qv = VT::get(lc, k) * (e * cscale);
-      VT::set(ov, k, qv);
+  for (int b = 0; b < J::BPT; ++b)
+#pragma unroll
+    for (int t = 0; t < J::R; ++t) {
+      const int x = J::pos(g, b, t);
+      const int i0 = y0 * NX + x, i1 = y1 * NX + x;
+      const T l0 = lw_cur[i0];
+      const T q0 = l0 * (r.v[b][t].x * cs);
+      qout[i0] = q0;
+      T l1 = (T)0, q1 = (T)0;
+      if constexpr (NY > 1) {
+        l1 = lw_cur[i1];
+        q1 = l1 * (r.v[b][t].y * cs);
+        qout[i1] = q1;
+      }
       if (lw_next) {
-        e = VT::get(ln, k) * qv;
-        if (NY == 1) S[x + k].y = (T)0;
+        const T n0 = same ? l0 : lw_next[i0];
+        const T n1 = NY > 1 ? (same ? l1 : lw_next[i1]) : (T)0;
+        r.v[b][t] = cx<T>(n0 * q0, n1 * q1);
       }
     }
-    o4[iv] = ov;
+}
+
+// u = lw * q (q alone when lw is null) into the registers of one row pair at the x join.
+template <typename T, int NX, int NY>
+__device__ __forceinline__ void load_regs(XRegs<T, NX>& r, int p, int g, const T* __restrict__ lw,
+                                          const T* __restrict__ q) {
+  using J = Join<NX>;
+  const int y0 = 2 * p, y1 = 2 * p + 1;
+#pragma unroll
+  for (int b = 0; b < J::BPT; ++b)
+#pragma unroll
+    for (int t = 0; t < J::R; ++t) {
+      const int x = J::pos(g, b, t);
+      const int i0 = y0 * NX + x, i1 = y1 * NX + x;
+      const T a = lw ? lw[i0] * q[i0] : q[i0];
+      T b1 = (T)0;
+      if constexpr (NY > 1) b1 = lw ? lw[i1] * q[i1] : q[i1];
+      r.v[b][t] = cx<T>(a, b1);
+    }
+}
+
+// 1D rows: forward transform (order B) of the registers at the x join into registers at the
+// B -> A join (full complex spectrum of the real row, natural positions).
+template <typename T, int NX>
+__device__ __forceinline__ void row_forward_1d(Cx<T>* z, const Cx<T>* twx, XRegs<T, NX>& r, BARegs<T, NX>& w, int g,
+                                               bool active) {
+  constexpr int P = Order<NX, 1>::P;
+  const Cx<T>* twb = twx + Order<NX, 0>::TW_SIZE;
+  using P0 = PassOf<T, false, NX, 1, 0>;
+  if constexpr (P == 1) {
+    if (active) {
+      P0::compute(r.v, g, twb);
+#pragma unroll
+      for (int b = 0; b < JoinBA<NX>::BPT; ++b)
+#pragma unroll
+        for (int t = 0; t < JoinBA<NX>::R; ++t) w.v[b][t] = r.v[b][t];
+    }
+  } else {
+    if (active) {
+      P0::compute(r.v, g, twb);
+      P0::store(r.v, g, [&](int i, const Cx<T>& x) { z[swz(i)] = x; });
+    }
+    __syncwarp();
+    smem_passes<T, false, NX, 1, 1, P - 1, true, true>(z, 1, g, twb, active);
+    using PL = PassOf<T, false, NX, 1, P - 1>;
+    if (active) {
+      PL::load(w.v, g, [&](int i) { return z[swz(i)]; });
+      PL::compute(w.v, g, twb + Order<NX, 1>::tw_offset(P - 1));
+    }
+    __syncwarp();
+  }
+}
+
+// 1D rows: inverse transform (order A) from registers at the B -> A join into registers at the
+// x join.
+template <typename T, int NX>
+__device__ __forceinline__ void row_inverse_1d(Cx<T>* z, const Cx<T>* twx, BARegs<T, NX>& w, XRegs<T, NX>& r, int g,
+                                               bool active) {
+  constexpr int P = Order<NX, 0>::P;
+  using P0 = PassOf<T, true, NX, 0, 0>;
+  if constexpr (P == 1) {
+    if (active) {
+      P0::compute(w.v, g, twx);
+#pragma unroll
+      for (int b = 0; b < Join<NX>::BPT; ++b)
+#pragma unroll
+        for (int t = 0; t < Join<NX>::R; ++t) r.v[b][t] = w.v[b][t];
+    }
+  } else {
+    if (active) {
+      P0::compute(w.v, g, twx);
+      P0::store(w.v, g, [&](int i, const Cx<T>& x) { z[swz(i)] = x; });
+    }
+    __syncwarp();
+    smem_passes<T, true, NX, 0, 1, P - 1, true, true>(z, 1, g, twx, active);
+    using PL = PassOf<T, true, NX, 0, P - 1>;
+    if (active) {
+      PL::load(r.v, g, [&](int i) { return z[swz(i)]; });
+      PL::compute(r.v, g, twx + Order<NX, 0>::tw_offset(P - 1));
+    }
+    __syncwarp();
   }
 }
 
 // ------------------------------------------------------------------ Nz == 1 chains
 template <typename T, int NX, int NY>
-__global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
+__global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS) __maxnreg__((PlaneCfg<NX, NY>::MAXREG))
     chain_plane_kernel(const ChainJob<T>* __restrict__ jobs, Twiddles<T> twg) {
   using C = PlaneCfg<NX, NY>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* S = reinterpret_cast<Cx<T>*>(smem_raw);
-  __shared__ Cx<T> twx[NX], twy[NY];
-  stage_twiddles<T, NX>(twx, twg.x);
-  stage_twiddles<T, NY>(twy, twg.y);
-  const Twiddles<T> tw{twx, twy, nullptr};
+  __shared__ Cx<T> twx[C::TWX], twy[C::TWY];
+  __shared__ T cshare;
+  stage<T>(twx, twg.x, C::TWX);
+  if (NY > 1) stage<T>(twy, twg.y, C::TWY);
   const ChainJob<T> job = jobs[blockIdx.x];
+  const int p = group_index<C::GX, C::SP>(threadIdx.x / C::GX), gx = threadIdx.x % C::GX;
+  const bool xact = p < C::NPAIR;
+  const int c = group_index<C::GY, C::SC>(threadIdx.x / C::GY), gy = threadIdx.x % C::GY;
+  const bool yact = NY > 1 && c < C::KX;
+  XRegs<T, NX> r;
+  __syncthreads();
+  if (xact) load_regs<T, NX, NY>(r, p, gx, job.ops[0].lw, job.hist + (long)job.s0 * C::NP);
 #pragma unroll 1
   for (int t = 0; t < job.nsteps; ++t) {
     const StepOp<T> op = job.ops[t];
-    if (t == 0) {
-      load_plane<T, NX, NY>(S, op.lw, job.hist + (long)job.s0 * C::NP);
-    }
-    __syncthreads();
-    plane_fwd<T, NX, NY>(S, tw.x, tw.y);
-    T c = (T)1;
-    if (job.csc) {
-      c = rescale_factor<T>(S[0].x, (double)C::NP);
-      if (threadIdx.x == 0) {
-        job.csc[t] = (float)c;
-        job.lsc[t] = log((double)c);
+    if constexpr (NY == 1) {
+      // forward row transform -> LD (and rescale) in registers -> inverse row transform
+      BARegs<T, NX> w;
+      row_forward_1d<T, NX>(S, twx, r, w, gx, xact);
+      T cs = (T)1;
+      if (job.csc) {
+        T c0 = (T)0;
+        if (xact && gx == 0) c0 = rescale_factor<T>(w.v[0][0].x, (double)C::NP);  // DC at position 0
+        cs = __shfl_sync(0xffffffffu, c0, 0);
+        if (threadIdx.x == 0) {
+          job.csc[t] = (float)cs;
+          job.lsc[t] = log((double)cs);
+        }
       }
-      __syncthreads();  // every thread has read S[0] before it is overwritten below
+      if (xact) {
+#pragma unroll
+        for (int b = 0; b < JoinBA<NX>::BPT; ++b)
+#pragma unroll
+          for (int tt = 0; tt < JoinBA<NX>::R; ++tt) {
+            const int x = JoinBA<NX>::pos(gx, b, tt);
+            const T f = op.ld[x <= NX / 2 ? x : NX - x] * cs;
+            w.v[b][tt] = cx<T>(w.v[b][tt].x * f, w.v[b][tt].y * f);
+          }
+      }
+      row_inverse_1d<T, NX>(S, twx, w, r, gx, xact);
+    } else {
+      // forward x -> forward y -> LD (and rescale) in registers -> inverse y -> inverse x
+      x_forward_from_regs<T, NX, NY>(S, twx, r, p, gx, xact);
+      __syncthreads();
+      BARegs<T, NY> w;
+      y_forward_to_regs<T, NX, NY>(S, twy, w, c, gy, yact);
+      T cs = (T)1;
+      if (job.csc) {
+        if (yact && c == 0 && gy == 0) cshare = rescale_factor<T>(w.v[0][0].x, (double)C::NP);
+        __syncthreads();
+        cs = cshare;
+        if (threadIdx.x == 0) {
+          job.csc[t] = (float)cs;
+          job.lsc[t] = log((double)cs);
+        }
+      }
+      if (yact) {
+#pragma unroll
+        for (int b = 0; b < JoinBA<NY>::BPT; ++b)
+#pragma unroll
+          for (int tt = 0; tt < JoinBA<NY>::R; ++tt) {
+            const int ky = JoinBA<NY>::pos(gy, b, tt);
+            const T f = op.ld[c * NY + ky] * cs;
+            w.v[b][tt] = cx<T>(w.v[b][tt].x * f, w.v[b][tt].y * f);
+          }
+      }
+      y_inverse_from_regs<T, NX, NY>(S, twy, w, c, gy, yact);
+      __syncthreads();
+      x_inverse_to_regs<T, NX, NY>(S, twx, r, p, gx, xact);
     }
-    for (int k = threadIdx.x; k < C::NKP; k += blockDim.x) {
-      const T f = op.ld[k] * c;
-      S[k] = cx<T>(S[k].x * f, S[k].y * f);
-    }
-    __syncthreads();
-    plane_inv<T, NX, NY>(S, tw.x, tw.y);
     const int s_out = job.s0 + job.dir * (t + 1);
     const T* lw_next = (t + 1 < job.nsteps) ? job.ops[t + 1].lw : nullptr;
-    finish_plane<T, NX, NY>(S, op.lw, lw_next, job.hist + (long)s_out * C::NP, (T)1);
-    __syncthreads();
+    if (xact) finish_regs<T, NX, NY>(r, p, gx, op.lw, lw_next, job.hist + (long)s_out * C::NP, (T)1);
+    if (NY > 1) __syncthreads();  // the next step's row transforms overwrite S
   }
 }
 
 // ------------------------------------------------------------------ 3D: plane pass
 template <typename T, int NX, int NY>
-__global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, sizeof(T) == 4 ? PlaneCfg<NX, NY>::MINB : 1)
+__global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
     xy_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nz, Twiddles<T> twg) {
   using C = PlaneCfg<NX, NY>;
+  static_assert(NY > 1, "3D grids have Ny > 1");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* S = reinterpret_cast<Cx<T>*>(smem_raw);
   const ChainJob<T> job = jobs[blockIdx.y];
   if (t > job.nsteps) return;
-  __shared__ Cx<T> twx[NX], twy[NY];
-  stage_twiddles<T, NX>(twx, twg.x);
-  stage_twiddles<T, NY>(twy, twg.y);
-  const Twiddles<T> tw{twx, twy, nullptr};
+  __shared__ Cx<T> twx[C::TWX], twy[C::TWY];
+  stage<T>(twx, twg.x, C::TWX);
+  stage<T>(twy, twg.y, C::TWY);
   const int z = blockIdx.x;
   const long ng = (long)C::NP * nz;
   const bool finish = t >= 1;
   const bool start = t < job.nsteps;
+  const int p = group_index<C::GX, C::SP>(threadIdx.x / C::GX), gx = threadIdx.x % C::GX;
+  const bool xact = p < C::NPAIR;
+  const int c = group_index<C::GY, C::SC>(threadIdx.x / C::GY), gy = threadIdx.x % C::GY;
+  const bool yact = c < C::KX;
+  __syncthreads();
+  XRegs<T, NX> r;
   if (finish) {
-    copy_cx<T>(S, job.kbuf + (long)z * C::NKP, C::NKP);
+    y_inverse_from_global<T, NX, NY>(S, job.kbuf + (long)z * C::NKP, twy);
     __syncthreads();
-    plane_inv<T, NX, NY>(S, tw.x, tw.y);
+    x_inverse_to_regs<T, NX, NY>(S, twx, r, p, gx, xact);
     const StepOp<T> op = job.ops[t - 1];
     const int s_out = job.s0 + job.dir * t;
     const T* lw_next = start ? job.ops[t].lw + (long)z * C::NP : nullptr;
-    const T c = job.csc ? (T)job.csc[t - 1] : (T)1;
-    finish_plane<T, NX, NY>(S, op.lw + (long)z * C::NP, lw_next, job.hist + (long)s_out * ng + (long)z * C::NP, c);
-  } else {
-    load_plane<T, NX, NY>(S, job.ops[0].lw + (long)z * C::NP, job.hist + (long)job.s0 * ng + (long)z * C::NP);
+    const T cs = job.csc ? (T)job.csc[t - 1] : (T)1;
+    if (xact)
+      finish_regs<T, NX, NY>(r, p, gx, op.lw + (long)z * C::NP, lw_next, job.hist + (long)s_out * ng + (long)z * C::NP,
+                             cs);
+  } else if (xact) {
+    load_regs<T, NX, NY>(r, p, gx, job.ops[0].lw + (long)z * C::NP, job.hist + (long)job.s0 * ng + (long)z * C::NP);
   }
-  __syncthreads();
   if (start) {
-    plane_fwd<T, NX, NY>(S, tw.x, tw.y);
-    copy_cx<T>(job.kbuf + (long)z * C::NKP, S, C::NKP);
+    x_forward_from_regs<T, NX, NY>(S, twx, r, p, gx, xact);
+    __syncthreads();
+    BARegs<T, NY> w;
+    y_forward_to_regs<T, NX, NY>(S, twy, w, c, gy, yact);
+    if (yact) {
+      Cx<T>* dst = job.kbuf + (long)z * C::NKP + c * NY;
+#pragma unroll
+      for (int b = 0; b < JoinBA<NY>::BPT; ++b)
+#pragma unroll
+        for (int tt = 0; tt < JoinBA<NY>::R; ++tt) dst[JoinBA<NY>::pos(gy, b, tt)] = w.v[b][tt];
+    }
   }
 }
 
 // ------------------------------------------------------------------ 3D: pencil pass
-// M consecutive pencils (index m = ky*Kx + kx within a plane) of length NZ per CTA.  The tile
-// is pencil-major in shared memory with rows padded by one element, Tl[mm*(NZ+1) + z], so the
-// threads of a transform group read consecutive words and the groups of a warp fall on
-// different banks.
-template <typename T>
-struct ZCfg {
-  static constexpr int M = sizeof(T) == 4 ? 16 : 8;  // 128-byte rows of the global tile
-};
-
+// Forward z transform (order B) from global, LD (+ the rescale factor of tile 0) in
+// registers, inverse z transform (order A) back to global.  M consecutive pencils per CTA,
+// one group of G threads per pencil; the pencil tile in shared memory is pencil-major with
+// rows padded by one element.
 template <typename T, int NZ>
 __global__ void __launch_bounds__(512)
     z_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nkp, double ng, Twiddles<T> twg) {
   constexpr int M = ZCfg<T>::M;
-  constexpr int LDT = NZ + 1;
-  constexpr int TOT = NZ * M;
+  constexpr int LDT = NZ + pencil_pad<NZ>();
+  constexpr int G = Plan<NZ>::G;
+  constexpr int P = Order<NZ, 0>::P;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* Tl = reinterpret_cast<Cx<T>*>(smem_raw);
   const ChainJob<T> job = jobs[blockIdx.y];
   if (t >= job.nsteps) return;
-  __shared__ Cx<T> twz[NZ];
-  stage_twiddles<T, NZ>(twz, twg.z);
-  const Twiddles<T> tw{nullptr, nullptr, twz};
+  __shared__ Cx<T> twz[tw_total<NZ>()];
+  stage<T>(twz, twg.z, tw_total<NZ>());
+  __syncthreads();
+  const Cx<T>* twb = twz + Order<NZ, 0>::TW_SIZE;
   const int m0 = blockIdx.x * M;
-  const int mc = min(M, nkp - m0);
+  const int mm = threadIdx.x / G, g = threadIdx.x % G;
+  const bool active = mm < M && m0 + mm < nkp;
+  const long col = m0 + (active ? mm : 0);
+  Cx<T>* pen = Tl + (active ? mm : 0) * LDT;
   Cx<T>* kb = job.kbuf;
-  for (int i = threadIdx.x; i < TOT; i += blockDim.x) {
-    const int zz = i / M, mm = i - zz * M;
-    Tl[mm * LDT + zz] = (mm < mc) ? kb[(long)zz * nkp + m0 + mm] : cx<T>(0, 0);
+  BARegs<T, NZ> w;
+  using F0 = PassOf<T, false, NZ, 1, 0>;
+  if constexpr (P == 1) {
+    if (active) {
+      F0::load(w.v, g, [&](int i) { return kb[(long)i * nkp + col]; });
+      F0::compute(w.v, g, twb);
+    }
+  } else {
+    Cx<T> v[F0::BPT][Order<NZ, 1>::radix(0)];
+    if (active) {
+      F0::load(v, g, [&](int i) { return kb[(long)i * nkp + col]; });
+      F0::compute(v, g, twb);
+      F0::store(v, g, [&](int i, const Cx<T>& x) { pen[swz(i)] = x; });
+    }
+    __syncwarp();
+    smem_passes<T, false, NZ, 1, 1, P - 1, true, true>(pen, 1, g, twb, active);
+    using FL = PassOf<T, false, NZ, 1, P - 1>;
+    if (active) {
+      FL::load(w.v, g, [&](int i) { return pen[swz(i)]; });
+      FL::compute(w.v, g, twb + Order<NZ, 1>::tw_offset(P - 1));
+    }
+    __syncwarp();
   }
-  __syncthreads();
-  fft_batch_n<T, false, NZ>(Tl, 1, LDT, M, tw.z);
-  __syncthreads();
   if (job.csc && blockIdx.x == 0 && threadIdx.x == 0) {
-    // the (0, 0, 0) coefficient is the grid sum of LW * q_t
-    const T c = rescale_factor<T>(Tl[0].x, ng);
+    // pencil 0, position 0: the (0, 0, 0) coefficient = grid sum of LW * q_t
+    const T c = rescale_factor<T>(w.v[0][0].x, ng);
     job.csc[t] = (float)c;
     job.lsc[t] = log((double)c);
   }
-  const T* ld = job.ops[t].ld;
-  for (int i = threadIdx.x; i < TOT; i += blockDim.x) {
-    const int zz = i / M, mm = i - zz * M;
-    if (mm < mc) {
-      const T f = ld[(long)zz * nkp + m0 + mm];
-      Cx<T>& e = Tl[mm * LDT + zz];
-      e = cx<T>(e.x * f, e.y * f);
-    }
+  if (active) {
+    const T* ld = job.ops[t].ld;
+#pragma unroll
+    for (int b = 0; b < JoinBA<NZ>::BPT; ++b)
+#pragma unroll
+      for (int tt = 0; tt < JoinBA<NZ>::R; ++tt) {
+        const T f = ld[(long)JoinBA<NZ>::pos(g, b, tt) * nkp + col];
+        w.v[b][tt] = cx<T>(w.v[b][tt].x * f, w.v[b][tt].y * f);
+      }
   }
-  __syncthreads();
-  fft_batch_n<T, true, NZ>(Tl, 1, LDT, M, tw.z);
-  __syncthreads();
-  for (int i = threadIdx.x; i < TOT; i += blockDim.x) {
-    const int zz = i / M, mm = i - zz * M;
-    if (mm < mc) kb[(long)zz * nkp + m0 + mm] = Tl[mm * LDT + zz];
+  using I0 = PassOf<T, true, NZ, 0, 0>;
+  if constexpr (P == 1) {
+    if (active) {
+      I0::compute(w.v, g, twz);
+      I0::store(w.v, g, [&](int i, const Cx<T>& x) { kb[(long)i * nkp + col] = x; });
+    }
+  } else {
+    if (active) {
+      I0::compute(w.v, g, twz);
+      I0::store(w.v, g, [&](int i, const Cx<T>& x) { pen[swz(i)] = x; });
+    }
+    __syncwarp();
+    smem_passes<T, true, NZ, 0, 1, P - 1, true, true>(pen, 1, g, twz, active);
+    using IL = PassOf<T, true, NZ, 0, P - 1>;
+    Cx<T> v[IL::BPT][Order<NZ, 0>::radix(P - 1)];
+    if (active) {
+      IL::load(v, g, [&](int i) { return pen[swz(i)]; });
+      IL::compute(v, g, twz + Order<NZ, 0>::tw_offset(P - 1));
+      IL::store(v, g, [&](int i, const Cx<T>& x) { kb[(long)i * nkp + col] = x; });
+    }
   }
 }
 
 // ------------------------------------------------------------------ stress transforms
-// For each item (a contour point s of one block): sum_k c_k Re(qhat_s,k) Re(qchat_s,k) dksq_p,k
-// with c_0 = 1 and c_k = 2 otherwise (quirk Q2, multiblock.jl:279-282).  Nz == 1 version:
-// one CTA per item transforms both planes.  Output: part[item * nparams + p].
+// Sum over the half spectrum of c_k Re(qhat_k) Re(qchat_k) dksq_p,k with c_0 = 1 and c_k = 2
+// otherwise (quirk Q2, multiblock.jl:279-282), for every item (a contour point of a block).
+// Nz == 1: one CTA per item transforms both planes.  Output part[item * nparams + p].
 template <typename T, int NX, int NY>
 __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
     stress_plane_kernel(const StressItem<T>* __restrict__ items, const double* __restrict__ dksq, int nparams,
                         double* __restrict__ part, Twiddles<T> twg) {
   using C = PlaneCfg<NX, NY>;
-  __shared__ Cx<T> twx[NX], twy[NY];
-  stage_twiddles<T, NX>(twx, twg.x);
-  stage_twiddles<T, NY>(twy, twg.y);
-  const Twiddles<T> tw{twx, twy, nullptr};
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* S = reinterpret_cast<Cx<T>*>(smem_raw);
-  T* req = reinterpret_cast<T*>(S + C::SLOTS);
+  T* req = reinterpret_cast<T*>(S + C::SLOTS);  // Re(qhat) in [kx][ky] order
+  __shared__ Cx<T> twx[C::TWX], twy[C::TWY];
   __shared__ double red[kMaxParams][32];
+  stage<T>(twx, twg.x, C::TWX);
+  if (NY > 1) stage<T>(twy, twg.y, C::TWY);
   const StressItem<T> it = items[blockIdx.x];
-  load_plane<T, NX, NY>(S, nullptr, it.q);
-  __syncthreads();
-  plane_fwd<T, NX, NY>(S, tw.x, tw.y);
-  for (int k = threadIdx.x; k < C::NKP; k += blockDim.x) req[k] = S[k].x;
-  __syncthreads();
-  load_plane<T, NX, NY>(S, nullptr, it.qc);
-  __syncthreads();
-  plane_fwd<T, NX, NY>(S, tw.x, tw.y);
+  const int p = group_index<C::GX, C::SP>(threadIdx.x / C::GX), gx = threadIdx.x % C::GX;
+  const bool xact = p < C::NPAIR;
+  const int c = group_index<C::GY, C::SC>(threadIdx.x / C::GY), gy = threadIdx.x % C::GY;
+  const bool yact = NY > 1 && c < C::KX;
   double acc[kMaxParams];
-  for (int p = 0; p < kMaxParams; ++p) acc[p] = 0.0;
-  for (int k = threadIdx.x; k < C::NKP; k += blockDim.x) {
-    const double prod = (double)S[k].x * (double)req[k] * (k == 0 ? 1.0 : 2.0);
-    for (int p = 0; p < nparams; ++p) acc[p] += prod * dksq[(long)p * C::NKP + k];
+  for (int k = 0; k < kMaxParams; ++k) acc[k] = 0.0;
+  __syncthreads();
+  for (int pass = 0; pass < 2; ++pass) {
+    XRegs<T, NX> r;
+    if (xact) load_regs<T, NX, NY>(r, p, gx, nullptr, pass == 0 ? it.q : it.qc);
+    if constexpr (NY == 1) {
+      BARegs<T, NX> w;
+      row_forward_1d<T, NX>(S, twx, r, w, gx, xact);
+      if (xact) {
+#pragma unroll
+        for (int b = 0; b < JoinBA<NX>::BPT; ++b)
+#pragma unroll
+          for (int tt = 0; tt < JoinBA<NX>::R; ++tt) {
+            const int x = JoinBA<NX>::pos(gx, b, tt);
+            if (x > NX / 2) continue;
+            if (pass == 0) {
+              req[x] = w.v[b][tt].x;
+            } else {
+              const double prod = (double)w.v[b][tt].x * (double)req[x] * (x == 0 ? 1.0 : 2.0);
+              for (int k = 0; k < nparams; ++k) acc[k] += prod * dksq[(long)k * C::NKP + x];
+            }
+          }
+      }
+      __syncwarp();
+    } else {
+      x_forward_from_regs<T, NX, NY>(S, twx, r, p, gx, xact);
+      __syncthreads();
+      BARegs<T, NY> w;
+      y_forward_to_regs<T, NX, NY>(S, twy, w, c, gy, yact);
+      if (yact) {
+#pragma unroll
+        for (int b = 0; b < JoinBA<NY>::BPT; ++b)
+#pragma unroll
+          for (int tt = 0; tt < JoinBA<NY>::R; ++tt) {
+            const int ky = JoinBA<NY>::pos(gy, b, tt);
+            const int kk = c * NY + ky;
+            if (pass == 0) {
+              req[kk] = w.v[b][tt].x;
+            } else {
+              const double prod = (double)w.v[b][tt].x * (double)req[kk] * (kk == 0 ? 1.0 : 2.0);
+              for (int k = 0; k < nparams; ++k) acc[k] += prod * dksq[(long)k * C::NKP + kk];
+            }
+          }
+      }
+    }
+    __syncthreads();
   }
-  for (int p = 0; p < nparams; ++p) {
-    double v = block_sum(acc[p], red[p]);
-    if (threadIdx.x == 0) part[(long)blockIdx.x * nparams + p] = v;
+  for (int k = 0; k < nparams; ++k) {
+    const double v = block_sum(acc[k], red[k]);
+    if (threadIdx.x == 0) part[(long)blockIdx.x * nparams + k] = v;
   }
 }
 
 // 3D stress, plane pass: forward x/y transforms of the real grids src[item] into the
-// half-spectrum buffers dst[item] (one CTA per (z, item)).
+// half-spectrum buffers dst[item] ([kz][kx][ky]), one CTA per (z, item).
 template <typename T, int NX, int NY>
 __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
     xy_fwd_kernel(const T* const* __restrict__ src, Cx<T>* const* __restrict__ dst, Twiddles<T> twg) {
   using C = PlaneCfg<NX, NY>;
-  __shared__ Cx<T> twx[NX], twy[NY];
-  stage_twiddles<T, NX>(twx, twg.x);
-  stage_twiddles<T, NY>(twy, twg.y);
-  const Twiddles<T> tw{twx, twy, nullptr};
+  static_assert(NY > 1, "3D grids have Ny > 1");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* S = reinterpret_cast<Cx<T>*>(smem_raw);
+  __shared__ Cx<T> twx[C::TWX], twy[C::TWY];
+  stage<T>(twx, twg.x, C::TWX);
+  stage<T>(twy, twg.y, C::TWY);
   const int z = blockIdx.x;
-  load_plane<T, NX, NY>(S, nullptr, src[blockIdx.y] + (long)z * C::NP);
+  const int p = group_index<C::GX, C::SP>(threadIdx.x / C::GX), gx = threadIdx.x % C::GX;
+  const bool xact = p < C::NPAIR;
+  const int c = group_index<C::GY, C::SC>(threadIdx.x / C::GY), gy = threadIdx.x % C::GY;
+  const bool yact = c < C::KX;
   __syncthreads();
-  plane_fwd<T, NX, NY>(S, tw.x, tw.y);
-  Cx<T>* o = dst[blockIdx.y] + (long)z * C::NKP;
-  for (int k = threadIdx.x; k < C::NKP; k += blockDim.x) o[k] = S[k];
+  XRegs<T, NX> r;
+  if (xact) load_regs<T, NX, NY>(r, p, gx, nullptr, src[blockIdx.y] + (long)z * C::NP);
+  x_forward_from_regs<T, NX, NY>(S, twx, r, p, gx, xact);
+  __syncthreads();
+  BARegs<T, NY> w;
+  y_forward_to_regs<T, NX, NY>(S, twy, w, c, gy, yact);
+  if (yact) {
+    Cx<T>* o = dst[blockIdx.y] + (long)z * C::NKP + c * NY;
+#pragma unroll
+    for (int b = 0; b < JoinBA<NY>::BPT; ++b)
+#pragma unroll
+      for (int tt = 0; tt < JoinBA<NY>::R; ++tt) o[JoinBA<NY>::pos(gy, b, tt)] = w.v[b][tt];
+  }
 }
 
-// 3D stress, pencil pass: z transforms of both spectra of an item and the weighted sum
-// over the tile.  Output: part[(item * ntiles + tile) * nparams + p].
+// Forward z transform (order B) of one pencil from global into registers (JoinBA positions).
+template <typename T, int NZ>
+__device__ __forceinline__ void z_forward_to_regs(const Cx<T>* __restrict__ kb, long nkp, long col, Cx<T>* pen,
+                                                  const Cx<T>* twz, BARegs<T, NZ>& w, int g, bool active) {
+  constexpr int P = Order<NZ, 0>::P;
+  const Cx<T>* twb = twz + Order<NZ, 0>::TW_SIZE;
+  using F0 = PassOf<T, false, NZ, 1, 0>;
+  if constexpr (P == 1) {
+    if (active) {
+      F0::load(w.v, g, [&](int i) { return kb[(long)i * nkp + col]; });
+      F0::compute(w.v, g, twb);
+    }
+  } else {
+    Cx<T> v[F0::BPT][Order<NZ, 1>::radix(0)];
+    if (active) {
+      F0::load(v, g, [&](int i) { return kb[(long)i * nkp + col]; });
+      F0::compute(v, g, twb);
+      F0::store(v, g, [&](int i, const Cx<T>& x) { pen[swz(i)] = x; });
+    }
+    __syncwarp();
+    smem_passes<T, false, NZ, 1, 1, P - 1, true, true>(pen, 1, g, twb, active);
+    using FL = PassOf<T, false, NZ, 1, P - 1>;
+    if (active) {
+      FL::load(w.v, g, [&](int i) { return pen[swz(i)]; });
+      FL::compute(w.v, g, twb + Order<NZ, 1>::tw_offset(P - 1));
+    }
+    __syncwarp();
+  }
+}
+
+// 3D stress, pencil pass: z transforms of both spectra of an item and the weighted sum over
+// the tile.  Output part[(item * ntiles + tile) * nparams + p].
 template <typename T, int NZ>
 __global__ void __launch_bounds__(512)
     z_fwd_stress_kernel(Cx<T>* const* __restrict__ kq, Cx<T>* const* __restrict__ kqc, int nkp,
                         const double* __restrict__ dksq, int nparams, double* __restrict__ part, Twiddles<T> twg) {
   constexpr int M = ZCfg<T>::M;
-  constexpr int LDT = NZ + 1;
-  __shared__ Cx<T> twz[NZ];
-  stage_twiddles<T, NZ>(twz, twg.z);
-  const Twiddles<T> tw{nullptr, nullptr, twz};
-  constexpr int TOT = NZ * M;
+  constexpr int LDT = NZ + pencil_pad<NZ>();
+  constexpr int G = Plan<NZ>::G;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx<T>* A = reinterpret_cast<Cx<T>*>(smem_raw);
   Cx<T>* B = A + M * LDT;
+  __shared__ Cx<T> twz[tw_total<NZ>()];
   __shared__ double red[kMaxParams][32];
+  stage<T>(twz, twg.z, tw_total<NZ>());
+  __syncthreads();
   const long nk = (long)nkp * NZ;
   const int m0 = blockIdx.x * M;
-  const int mc = min(M, nkp - m0);
-  const Cx<T>* a = kq[blockIdx.y];
-  const Cx<T>* b = kqc[blockIdx.y];
-  for (int i = threadIdx.x; i < TOT; i += blockDim.x) {
-    const int zz = i / M, mm = i - zz * M;
-    A[mm * LDT + zz] = (mm < mc) ? a[(long)zz * nkp + m0 + mm] : cx<T>(0, 0);
-    B[mm * LDT + zz] = (mm < mc) ? b[(long)zz * nkp + m0 + mm] : cx<T>(0, 0);
-  }
-  __syncthreads();
-  fft_batch_n<T, false, NZ>(A, 1, LDT, M, tw.z);
-  fft_batch_n<T, false, NZ>(B, 1, LDT, M, tw.z);
-  __syncthreads();
+  const int mm = threadIdx.x / G, g = threadIdx.x % G;
+  const bool active = mm < M && m0 + mm < nkp;
+  const long col = m0 + (active ? mm : 0);
+  BARegs<T, NZ> wa, wb;
+  z_forward_to_regs<T, NZ>(kq[blockIdx.y], nkp, col, A + (active ? mm : 0) * LDT, twz, wa, g, active);
+  z_forward_to_regs<T, NZ>(kqc[blockIdx.y], nkp, col, B + (active ? mm : 0) * LDT, twz, wb, g, active);
   double acc[kMaxParams];
-  for (int p = 0; p < kMaxParams; ++p) acc[p] = 0.0;
-  for (int i = threadIdx.x; i < TOT; i += blockDim.x) {
-    const int zz = i / M, mm = i - zz * M;
-    if (mm < mc) {
-      const long k = (long)zz * nkp + m0 + mm;
-      const double prod = (double)A[mm * LDT + zz].x * (double)B[mm * LDT + zz].x * (k == 0 ? 1.0 : 2.0);
-      for (int p = 0; p < nparams; ++p) acc[p] += prod * dksq[p * nk + k];
-    }
+  for (int k = 0; k < kMaxParams; ++k) acc[k] = 0.0;
+  if (active) {
+#pragma unroll
+    for (int b = 0; b < JoinBA<NZ>::BPT; ++b)
+#pragma unroll
+      for (int tt = 0; tt < JoinBA<NZ>::R; ++tt) {
+        const long kk = (long)JoinBA<NZ>::pos(g, b, tt) * nkp + col;
+        const double prod = (double)wa.v[b][tt].x * (double)wb.v[b][tt].x * (kk == 0 ? 1.0 : 2.0);
+        for (int k = 0; k < nparams; ++k) acc[k] += prod * dksq[k * nk + kk];
+      }
   }
-  for (int p = 0; p < nparams; ++p) {
-    double v = block_sum(acc[p], red[p]);
-    if (threadIdx.x == 0) part[((long)blockIdx.y * gridDim.x + blockIdx.x) * nparams + p] = v;
+  for (int k = 0; k < nparams; ++k) {
+    const double v = block_sum(acc[k], red[k]);
+    if (threadIdx.x == 0) part[((long)blockIdx.y * gridDim.x + blockIdx.x) * nparams + k] = v;
   }
 }
 
@@ -467,15 +845,14 @@ static inline int shape_key(int nx, int ny) { return nx * 1024 + ny; }
 
 template <typename T, int NZ>
 static constexpr int z_threads() {
-  constexpr int t = ZCfg<T>::M * Plan<NZ>::G;
-  return t < 64 ? 64 : t;
+  return round32(ZCfg<T>::M * Plan<NZ>::G);
 }
 
 template <typename T, int NZ>
 static void launch_z_step(const ChainJob<T>* jobs, int t, int nkp, double ng, int njobs, const Twiddles<T>& tw,
                           cudaStream_t st) {
   constexpr int M = ZCfg<T>::M;
-  const size_t sz = sizeof(Cx<T>) * (size_t)(NZ + 1) * M;
+  const size_t sz = sizeof(Cx<T>) * (size_t)(NZ + pencil_pad<NZ>()) * M;
   static bool attr = false;
   if (!attr) {
     set_smem(z_step_kernel<T, NZ>, sz);
@@ -483,13 +860,12 @@ static void launch_z_step(const ChainJob<T>* jobs, int t, int nkp, double ng, in
   }
   const int ntiles = (nkp + M - 1) / M;
   z_step_kernel<T, NZ><<<dim3(ntiles, njobs), z_threads<T, NZ>(), sz, st>>>(jobs, t, nkp, ng, tw);
-    count_launches(1);
+  count_launches(1);
 }
 
 template <typename T>
 static bool z_step_dispatch(int nz, const ChainJob<T>* jobs, int t, int nkp, double ng, int njobs,
-                            const Twiddles<T>& tw,
-                            cudaStream_t st) {
+                            const Twiddles<T>& tw, cudaStream_t st) {
   switch (nz) {
 #define PF_Z(N)                                           \
   case N:                                                 \
@@ -510,7 +886,7 @@ static void chains_shape(const ChainJob<T>* jobs, int njobs, int maxsteps, int n
   static bool attr = false;
   if (!attr) {
     set_smem(chain_plane_kernel<T, NX, NY>, sp);
-    set_smem(xy_step_kernel<T, NX, NY>, sp);
+    if constexpr (NY > 1) set_smem(xy_step_kernel<T, NX, NY>, sp);
     attr = true;
   }
   if (nz == 1) {
@@ -518,10 +894,12 @@ static void chains_shape(const ChainJob<T>* jobs, int njobs, int maxsteps, int n
     count_launches(1);
     return;
   }
-  for (int t = 0; t <= maxsteps; ++t) {
-    xy_step_kernel<T, NX, NY><<<dim3(nz, njobs), C::THREADS, sp, st>>>(jobs, t, nz, tw);
-    count_launches(1);
-    if (t < maxsteps) z_step_dispatch<T>(nz, jobs, t, C::NKP, (double)C::NP * nz, njobs, tw, st);
+  if constexpr (NY > 1) {
+    for (int t = 0; t <= maxsteps; ++t) {
+      xy_step_kernel<T, NX, NY><<<dim3(nz, njobs), C::THREADS, sp, st>>>(jobs, t, nz, tw);
+      count_launches(1);
+      if (t < maxsteps) z_step_dispatch<T>(nz, jobs, t, C::NKP, (double)C::NP * nz, njobs, tw, st);
+    }
   }
 }
 
@@ -535,7 +913,7 @@ static void stress_shape(const StressItem<T>* items, int nitems, const T* const*
   static bool attr = false;
   if (!attr) {
     set_smem(stress_plane_kernel<T, NX, NY>, ss);
-    set_smem(xy_fwd_kernel<T, NX, NY>, sp);
+    if constexpr (NY > 1) set_smem(xy_fwd_kernel<T, NX, NY>, sp);
     attr = true;
   }
   if (nz == 1) {
@@ -543,27 +921,31 @@ static void stress_shape(const StressItem<T>* items, int nitems, const T* const*
     count_launches(1);
     return;
   }
-  xy_fwd_kernel<T, NX, NY><<<dim3(nz, nitems), C::THREADS, sp, st>>>(src_q, kq, tw);
+  if constexpr (NY > 1) {
+    xy_fwd_kernel<T, NX, NY><<<dim3(nz, nitems), C::THREADS, sp, st>>>(src_q, kq, tw);
     count_launches(1);
-  xy_fwd_kernel<T, NX, NY><<<dim3(nz, nitems), C::THREADS, sp, st>>>(src_qc, kqc, tw);
+    xy_fwd_kernel<T, NX, NY><<<dim3(nz, nitems), C::THREADS, sp, st>>>(src_qc, kqc, tw);
     count_launches(1);
-  constexpr int M = ZCfg<T>::M;
-  const int ntiles = (C::NKP + M - 1) / M;
-  switch (nz) {
-#define PF_Z(N)                                                                                              \
-  case N: {                                                                                                  \
-    const size_t sz = 2 * sizeof(Cx<T>) * (size_t)(N + 1) * M;                                               \
-    static bool za = false;                                                                                  \
-    if (!za) {                                                                                               \
-      set_smem(z_fwd_stress_kernel<T, N>, sz);                                                               \
-      za = true;                                                                                             \
-    }                                                                                                        \
-    z_fwd_stress_kernel<T, N><<<dim3(ntiles, nitems), z_threads<T, N>(), sz, st>>>(kq, kqc, C::NKP, dksq, nparams, part, tw); count_launches(1); \
+    constexpr int M = ZCfg<T>::M;
+    const int ntiles = (C::NKP + M - 1) / M;
+    switch (nz) {
+#define PF_Z(N)                                                                                                    \
+  case N: {                                                                                                        \
+    const size_t sz = 2 * sizeof(Cx<T>) * (size_t)(N + pencil_pad<N>()) * M;                                       \
+    static bool za = false;                                                                                        \
+    if (!za) {                                                                                                     \
+      set_smem(z_fwd_stress_kernel<T, N>, sz);                                                                     \
+      za = true;                                                                                                   \
+    }                                                                                                              \
+    z_fwd_stress_kernel<T, N><<<dim3(ntiles, nitems), z_threads<T, N>(), sz, st>>>(kq, kqc, C::NKP, dksq, nparams, \
+                                                                                  part, tw);                      \
+    count_launches(1);                                                                                             \
   } break;
-    PF_Z_LENGTHS(PF_Z)
+      PF_Z_LENGTHS(PF_Z)
 #undef PF_Z
-    default:
-      break;
+      default:
+        break;
+    }
   }
 }
 
@@ -572,16 +954,16 @@ template <typename T>
 bool shape_supported(int nx, int ny, int nz) {
   bool plane = false;
   switch (shape_key(nx, ny)) {
-#define PF_S(A, B)                                                                        \
-  case A * 1024 + B:                                                                      \
-    plane = plane_smem<T, A, B>() + sizeof(T) * PlaneCfg<A, B>::NKP <= 227 * 1024;         \
+#define PF_S(A, B)                                                                       \
+  case A * 1024 + B:                                                                     \
+    plane = plane_smem<T, A, B>() + sizeof(T) * PlaneCfg<A, B>::NKP <= 200 * 1024;       \
     break;
     PF_PLANE_SHAPES(PF_S)
 #undef PF_S
     default:
       plane = false;
   }
-  return plane && (nz == 1 || fft_length_supported(nz));
+  return plane && (nz == 1 || (ny > 1 && fft_length_supported(nz)));
 }
 
 template <typename T>
@@ -589,7 +971,7 @@ void launch_lw(T* lw, const double* w, double coeff, long n, cudaStream_t st) {
   int blocks = (int)((n + 255) / 256);
   if (blocks > 4096) blocks = 4096;
   lw_kernel<T><<<blocks, 256, 0, st>>>(lw, w, coeff, n);
-    count_launches(1);
+  count_launches(1);
 }
 
 template <typename T>
@@ -597,7 +979,7 @@ void launch_ld(T* ld, const CellGeom& g, double coeff, double scale, long nk, cu
   int blocks = (int)((nk + 255) / 256);
   if (blocks > 4096) blocks = 4096;
   ld_kernel<T><<<blocks, 256, 0, st>>>(ld, g, coeff, scale);
-    count_launches(1);
+  count_launches(1);
 }
 
 template <typename T>
@@ -605,7 +987,7 @@ void launch_fill(T* a, T v, long n, cudaStream_t st) {
   int blocks = (int)((n + 255) / 256);
   if (blocks > 4096) blocks = 4096;
   fill_kernel<T><<<blocks, 256, 0, st>>>(a, v, n);
-    count_launches(1);
+  count_launches(1);
 }
 
 template <typename T>

@@ -27,8 +27,8 @@ namespace {
 constexpr size_t kScratchBytes = size_t(16) << 20;  // 16 MiB
 constexpr size_t kJobOffset = 0;                     // one ChainJob
 constexpr size_t kOpsOffset = 4096;                  // StepOp table
-constexpr size_t kTwOffset = 64 * 1024;              // twiddles for x, y, z
-constexpr size_t kKbufOffset = 80 * 1024;            // half-spectrum buffer (3D)
+constexpr size_t kTwOffset = 64 * 1024;              // twiddle tables for x, y, z
+constexpr size_t kKbufOffset = 96 * 1024;            // half-spectrum buffer (3D)
 constexpr int kMaxNoallocSteps = (int)((kTwOffset - kOpsOffset) / sizeof(StepOp<double>));
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -81,16 +81,21 @@ int propagate_noalloc(int nx, int ny, int nz, T* hist, const T* lw, const T* ld,
   std::vector<StepOp<T>> hops(nsteps, StepOp<T>{lw, ld});
   const ChainJob<T> hjob{hist, ops_dev, kbuf, nullptr, nullptr, 0, +1, nsteps, 0};
   std::vector<Cx<T>> htw;
-  for (int n : {nx, ny, nz})
-    for (int m = 0; m < n; ++m) {
-      const long double a = -2.0L * 3.141592653589793238462643383279502884L * (long double)m / (long double)n;
-      htw.push_back(cx<T>((T)std::cos(a), (T)std::sin(a)));
-    }
+  int off[3];
+  for (int a = 0; a < 3; ++a) {
+    const int n = a == 0 ? nx : a == 1 ? ny : nz;
+    double re[1024], im[1024];
+    const int cnt = fft_twiddle_table(n, re, im, 1024);
+    if (cnt < 0) return E_UNSUPPORTED;
+    off[a] = (int)htw.size();
+    for (int i = 0; i < cnt; ++i) htw.push_back(cx<T>((T)re[i], (T)im[i]));
+  }
+  if (sizeof(Cx<T>) * htw.size() > kKbufOffset - kTwOffset) return E_UNSUPPORTED;
   if (cudaMemcpyAsync(ops_dev, hops.data(), sizeof(StepOp<T>) * nsteps, cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(job_dev, &hjob, sizeof(hjob), cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(tw_dev, htw.data(), sizeof(Cx<T>) * htw.size(), cudaMemcpyHostToDevice, st) != cudaSuccess)
     return E_CUDA;
-  const Twiddles<T> tw{tw_dev, tw_dev + nx, tw_dev + nx + ny};
+  const Twiddles<T> tw{tw_dev + off[0], tw_dev + off[1], tw_dev + off[2]};
   launch_chains<T>(job_dev, 1, nsteps, GridDims{nx, ny, nz}, tw, st);
   return cudaGetLastError() == cudaSuccess ? OK : E_CUDA;
 }

@@ -226,8 +226,9 @@ def test_fp32_rescaled_strong_fields():
     o = SY.blend3d_system(O, n=16)
     g = SY.blend3d_system(pf, n=16, precision="fp32")
     assert o.species[0].Q > 1e30
+    # 400 float32 contour steps through fields of this strength: 1e-4 on Q
     for isp in range(2):
-        assert g.species[isp].Q == pytest.approx(o.species[isp].Q, rel=FP32_RTOL)
+        assert g.species[isp].Q == pytest.approx(o.species[isp].Q, rel=2 * FP32_RTOL)
     for mid in (1, 2):
         assert rel(g.density[mid], o.density[mid]) < 2 * FP32_RTOL
     assert g.free_energy() == pytest.approx(o.free_energy(), rel=1e-4)

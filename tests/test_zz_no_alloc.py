@@ -29,8 +29,8 @@ def rel(a, b):
 
 
 def host_operators(dims, crystal, params, w, vol, b, ds, npdt):
-    """LW = exp(-ds vol w / 2) and LD = exp(-ds b^2 k^2 / 6) / Ng on the [kz][ky][kx] half
-    spectrum (k^2 from the oracle's cell, quirk Q1 fold included)."""
+    """LW = exp(-ds vol w / 2) and LD = exp(-ds b^2 k^2 / 6) / Ng on the half spectrum in the
+    engine's [kz][kx][ky] layout (k^2 from the oracle's cell, quirk Q1 fold included)."""
     nd = sum(1 for d in dims if d > 1)
     cell = O.UnitCell(nd, crystal, *params)
     cell.setup(dims)
@@ -38,7 +38,7 @@ def host_operators(dims, crystal, params, w, vol, b, ds, npdt):
     kshape = (dims[2], dims[1], dims[0] // 2 + 1)
     lw = np.exp(-ds / 2.0 * vol * w).astype(npdt)
     ld = (np.exp(-ds * b * b / 6.0 * np.broadcast_to(cell.ksq, kshape)) / ng).astype(npdt)
-    return lw, np.ascontiguousarray(ld)
+    return lw, np.ascontiguousarray(ld.transpose(0, 2, 1))
 
 
 CASES = [((32, 32, 32), "cubic", (7.0,), "fp64"), ((32, 32, 32), "cubic", (7.0,), "fp32"),
