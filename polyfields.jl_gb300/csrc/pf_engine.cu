@@ -7,6 +7,7 @@
 // scft! driver loop (src/simulate.jl:60-148).  The orchestration runs on the host; every
 // grid-sized operation runs on the device, on the handle's own stream.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -397,6 +398,11 @@ struct System {
   int njobs = 0, maxsteps = 0;
   bool jobs_dirty[2] = {true, true};
   bool timing = false;
+  // density solves replay a captured CUDA graph per precision (PF_NO_GRAPHS=1 disables)
+  bool use_graphs = true;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  bool graph_warm[2] = {false, false};
+  long graph_kernels[2] = {0, 0};
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t uev[8] = {};  // user events (pf_record_event)
   double t_prop_ms = 0.0, t_dens_ms = 0.0;
@@ -442,9 +448,12 @@ struct System {
     build_twiddles<float>(1);
     for (auto& e : ev) PF_CU(cudaEventCreate(&e));
     for (auto& e : uev) PF_CU(cudaEventCreate(&e));
+    const char* ng_env = getenv("PF_NO_GRAPHS");
+    if (ng_env && ng_env[0] == '1') use_graphs = false;
   }
   ~System() {
     if (st) cudaStreamSynchronize(st);
+    invalidate_graphs();
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     for (auto& e : uev)
@@ -534,6 +543,7 @@ struct System {
     }
     and_.reset();
     jobs_dirty[0] = jobs_dirty[1] = true;
+    invalidate_graphs();
   }
 
   void add_multiblock(int nb, const int* bm, const int* Nb, const double* bb, int Ns, double phi) {
@@ -561,6 +571,7 @@ struct System {
     sp->Qdev.alloc(sizeof(double));
     species.push_back(std::move(sp));
     jobs_dirty[0] = jobs_dirty[1] = true;
+    invalidate_graphs();
   }
 
   void add_point(int mid, double phi) {
@@ -574,6 +585,7 @@ struct System {
     sp->phi = phi;
     sp->Qdev.alloc(sizeof(double));
     species.push_back(std::move(sp));
+    invalidate_graphs();
   }
 
   void set_flory(int a, int b, double chi) {
@@ -614,6 +626,9 @@ struct System {
   template <typename T>
   void ensure_prop(int p) {
     if (!jobs_dirty[p]) return;
+    if (gexec[p]) cudaGraphExecDestroy(gexec[p]);
+    gexec[p] = nullptr;
+    graph_warm[p] = false;
     std::vector<ChainJob<T>> hjobs;
     maxsteps = 0;
     for (auto& spp : species) {
@@ -683,35 +698,32 @@ struct System {
     jobs_dirty[p] = false;
   }
 
-  // ---------------------------------------------------------------- density!(sys)
+  // ---------------------------------------------------------------- density solve body
+  bool capturing = false;
+  void record_ev(int i) {
+    if (capturing) PF_CU(cudaEventRecordWithFlags(ev[i], st, cudaEventRecordExternal));
+    else PF_CU(cudaEventRecord(ev[i], st));
+  }
+  // Everything of one density solve that depends only on device pointers fixed at setup:
+  // captured once per precision into a CUDA graph and replayed on later solves.  The timing
+  // events are recorded as external-event nodes so that replays record them too.
   template <typename T>
-  void density_t(int p) {
-    require_ready();
-    ensure_prop<T>(p);
-    const double invng = 1.0 / (double)ng;
+  void density_enqueue(int p) {
     PF_CU(cudaMemsetAsync(rho.p, 0, sizeof(double) * ng * nmon(), st));
-    if (timing) PF_CU(cudaEventRecord(ev[0], st));
-    const CellGeom g = geom();
-    mde_steps = 0;
+    record_ev(0);
     for (auto& spp : species) {
       Species& sp = *spp;
       if (sp.kind != 0) continue;
       for (int b = 0; b < sp.nblocks(); ++b) {
         const auto& m = monomers.at(sp.mid_block[b]);
         launch_lw<T>(sp.lw[p][b]->as<T>(), grid_ptr(w, sp.mid_block[b]), sp.ds_block[b] / 2.0 * m.first, ng, st);
-        if (sp.ld_version[p] != cell_version)
-          launch_ld<T>(sp.ld[p][b]->as<T>(), g, sp.ds_block[b] * sp.b_block[b] * sp.b_block[b] / 6.0, invng, nk, st);
       }
-      sp.ld_version[p] = cell_version;
       launch_fill<T>(sp.q[p].as<T>(), (T)1, ng, st);
       if (sp.nblocks() > 1) launch_fill<T>(sp.qc[p].as<T>() + (long)sp.Ns * ng, (T)1, ng, st);
-      mde_steps += sp.Ns * (sp.nblocks() > 1 ? 2 : 1);
     }
-    check_launch();
-    if (timing) PF_CU(cudaEventRecord(ev[1], st));
+    record_ev(1);
     if (njobs) launch_chains<T>(jobs[p].as<ChainJob<T>>(), njobs, maxsteps, GridDims{nx, ny, nz}, tw<T>(p), st);
-    check_launch();
-    if (timing) PF_CU(cudaEventRecord(ev[2], st));
+    record_ev(2);
     for (auto& spp : species) {
       Species& sp = *spp;
       if (sp.kind == 0) {
@@ -743,11 +755,63 @@ struct System {
         launch_point_q(grid_ptr(w, mid), vol, ng, part.as<double>(), sp.Qdev.as<double>(), st);
         launch_point_density(grid_ptr(rho, mid), grid_ptr(w, mid), vol, sp.phi, sp.Qdev.as<double>(), ng, st);
       }
-      sp.Q_valid = false;
+    }
+    record_ev(3);
+  }
+
+  // ---------------------------------------------------------------- density!(sys)
+  template <typename T>
+  void density_t(int p) {
+    require_ready();
+    ensure_prop<T>(p);
+    // bond operators: regenerated (outside the graph) when the cell changed
+    const CellGeom g = geom();
+    mde_steps = 0;
+    for (auto& spp : species) {
+      Species& sp = *spp;
+      if (sp.kind != 0) continue;
+      if (sp.ld_version[p] != cell_version)
+        for (int b = 0; b < sp.nblocks(); ++b)
+          launch_ld<T>(sp.ld[p][b]->as<T>(), g, sp.ds_block[b] * sp.b_block[b] * sp.b_block[b] / 6.0,
+                       1.0 / (double)ng, nk, st);
+      sp.ld_version[p] = cell_version;
+      mde_steps += sp.Ns * (sp.nblocks() > 1 ? 2 : 1);
     }
     check_launch();
+    if (!use_graphs) {
+      density_enqueue<T>(p);
+    } else if (gexec[p]) {
+      PF_CU(cudaGraphLaunch(gexec[p], st));
+      count_launches(graph_kernels[p]);
+    } else if (!graph_warm[p]) {
+      // first solve runs directly (it also sets the kernels' shared-memory attributes)
+      density_enqueue<T>(p);
+      graph_warm[p] = true;
+    } else {
+      const long l0 = launch_total();
+      PF_CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      capturing = true;
+      try {
+        density_enqueue<T>(p);
+      } catch (...) {
+        capturing = false;
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(st, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      capturing = false;
+      cudaGraph_t graph = nullptr;
+      PF_CU(cudaStreamEndCapture(st, &graph));
+      graph_kernels[p] = launch_total() - l0;
+      cudaError_t e = cudaGraphInstantiate(&gexec[p], graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) throw PFError(E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+      PF_CU(cudaGraphLaunch(gexec[p], st));
+    }
+    check_launch();
+    for (auto& sp : species) sp->Q_valid = false;
     if (timing) {
-      PF_CU(cudaEventRecord(ev[3], st));
       PF_CU(cudaEventSynchronize(ev[3]));
       float a = 0, b = 0;
       PF_CU(cudaEventElapsedTime(&a, ev[1], ev[2]));
@@ -756,6 +820,13 @@ struct System {
       t_dens_ms = b;
     }
     last_prec = p;
+  }
+  void invalidate_graphs() {
+    for (int p = 0; p < 2; ++p) {
+      if (gexec[p]) cudaGraphExecDestroy(gexec[p]);
+      gexec[p] = nullptr;
+      graph_warm[p] = false;
+    }
   }
   void density() {
     if (prec == 0) density_t<double>(0);

@@ -244,3 +244,26 @@ def test_fp32_propagator_accessor_unscaled():
     for s in (0, 7, 50, ch_o.Ns):
         assert rel(ch_g.propagator(s), ch_o.q[s]) < FP32_RTOL
         assert rel(ch_g.propagator(s, conjugate=True), ch_o.qc[s]) < FP32_RTOL
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_RTOL), ("fp32", FP32_RTOL)])
+def test_density_graph_replay_follows_fields_and_cell(prec, tol):
+    """From the third density solve on, the engine replays one captured CUDA graph per
+    precision.  New fields (read by the graph from the same buffers) and new cells (bond
+    operators regenerated outside the graph) must still give the oracle's densities."""
+    kw = dict(dims=(16, 16, 16), crystal="cubic", params=(6.0,), f=0.3, amp=0.15)
+    o = SY.diblock_system(O, **kw)
+    g = SY.diblock_system(pf, precision=prec, **kw)
+    shape = o.shape
+    for k in range(6):
+        if k in (3, 5):
+            o.add_cell(O.UnitCell(3, "cubic", 6.0 + 0.1 * k))
+            g.add_cell(pf.UnitCell(3, "cubic", 6.0 + 0.1 * k))
+        fields = SY.seeded_fields(shape, [1, 2], seed=200 + k, scale=0.2)
+        O.fieldinit(o, fields)
+        pf.fieldinit(g, fields)
+        o.density_update()
+        g.density_update()
+        assert g.species[0].Q == pytest.approx(o.species[0].Q, rel=tol), k
+        for mid in (1, 2):
+            assert rel(g.density[mid], o.density[mid]) < tol, (k, mid)
