@@ -396,6 +396,10 @@ struct System {
   DevBuf dksq;
   DevBuf jobs[2];
   int njobs = 0, maxsteps = 0;
+  // 3D chains run one branch stream per job (PF_NO_BRANCHES=1: all jobs in shared launches)
+  bool use_branches = true;
+  Branches br;
+  std::vector<int> job_steps;
   bool jobs_dirty[2] = {true, true};
   bool timing = false;
   // density solves replay a captured CUDA graph per precision (PF_NO_GRAPHS=1 disables)
@@ -450,6 +454,8 @@ struct System {
     for (auto& e : uev) PF_CU(cudaEventCreate(&e));
     const char* ng_env = getenv("PF_NO_GRAPHS");
     if (ng_env && ng_env[0] == '1') use_graphs = false;
+    const char* nb_env = getenv("PF_NO_BRANCHES");
+    if (nb_env && nb_env[0] == '1') use_branches = false;
   }
   ~System() {
     if (st) cudaStreamSynchronize(st);
@@ -458,7 +464,25 @@ struct System {
       if (e) cudaEventDestroy(e);
     for (auto& e : uev)
       if (e) cudaEventDestroy(e);
+    for (int b = 0; b < kMaxBranches; ++b) {
+      if (br.s[b]) cudaStreamDestroy(br.s[b]);
+      if (br.join[b]) cudaEventDestroy(br.join[b]);
+    }
+    if (br.fork) cudaEventDestroy(br.fork);
     if (st) cudaStreamDestroy(st);
+  }
+  // branch streams for njobs chains (created once, kept for the handle's lifetime)
+  const Branches* branches() {
+    if (!use_branches || nz == 1 || njobs < 2) return nullptr;
+    const int want = std::min(njobs, kMaxBranches);
+    if (!br.fork) PF_CU(cudaEventCreateWithFlags(&br.fork, cudaEventDisableTiming));
+    for (int b = 0; b < want; ++b) {
+      if (!br.s[b]) PF_CU(cudaStreamCreateWithFlags(&br.s[b], cudaStreamNonBlocking));
+      if (!br.join[b]) PF_CU(cudaEventCreateWithFlags(&br.join[b], cudaEventDisableTiming));
+    }
+    br.n = want;
+    br.steps = job_steps.data();
+    return &br;
   }
 
   int nmon() const { return (int)mon_ids.size(); }
@@ -693,6 +717,8 @@ struct System {
       maxsteps = std::max(maxsteps, sp.Ns);
     }
     njobs = (int)hjobs.size();
+    job_steps.clear();
+    for (const auto& j : hjobs) job_steps.push_back(j.nsteps);
     jobs[p].alloc(sizeof(ChainJob<T>) * std::max(1, njobs));
     if (njobs) PF_CU(cudaMemcpy(jobs[p].p, hjobs.data(), sizeof(ChainJob<T>) * njobs, cudaMemcpyHostToDevice));
     jobs_dirty[p] = false;
@@ -722,7 +748,8 @@ struct System {
       if (sp.nblocks() > 1) launch_fill<T>(sp.qc[p].as<T>() + (long)sp.Ns * ng, (T)1, ng, st);
     }
     record_ev(1);
-    if (njobs) launch_chains<T>(jobs[p].as<ChainJob<T>>(), njobs, maxsteps, GridDims{nx, ny, nz}, tw<T>(p), st);
+    if (njobs)
+      launch_chains<T>(jobs[p].as<ChainJob<T>>(), njobs, maxsteps, GridDims{nx, ny, nz}, tw<T>(p), st, branches());
     record_ev(2);
     for (auto& spp : species) {
       Species& sp = *spp;

@@ -85,9 +85,20 @@ template <typename T> void launch_lw(T* lw, const double* w, double coeff, long 
 template <typename T> void launch_ld(T* ld, const CellGeom& g, double coeff, double scale, long nk, cudaStream_t st);
 void launch_dksq(double* dk, const CellGeom& g, int nparams, long nk, cudaStream_t st);
 template <typename T> void launch_fill(T* a, T v, long n, cudaStream_t st);
+// Branch streams for 3D chains: with n > 0 each job advances on its own stream (job j on
+// s[j % n]), forked from the main stream by `fork` and joined back by join[], so that the plane
+// and pencil passes of independent chains overlap on the GPU.  steps[j] = job j's step count.
+constexpr int kMaxBranches = 8;
+struct Branches {
+  int n = 0;
+  cudaStream_t s[kMaxBranches] = {};
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join[kMaxBranches] = {};
+  const int* steps = nullptr;
+};
 template <typename T>
 void launch_chains(const ChainJob<T>* jobs_dev, int njobs, int maxsteps, const GridDims& d, const Twiddles<T>& tw,
-                   cudaStream_t st);
+                   cudaStream_t st, const Branches* br = nullptr);
 // Stress sums: Nz == 1 uses items (device array of nitems); 3D grids use the pointer arrays
 // src_q/src_qc (real grids) and kq/kqc (half-spectrum scratch), each nitems long.
 template <typename T>

@@ -880,7 +880,7 @@ static bool z_step_dispatch(int nz, const ChainJob<T>* jobs, int t, int nkp, dou
 
 template <typename T, int NX, int NY>
 static void chains_shape(const ChainJob<T>* jobs, int njobs, int maxsteps, int nz, const Twiddles<T>& tw,
-                         cudaStream_t st) {
+                         cudaStream_t st, const Branches* br) {
   using C = PlaneCfg<NX, NY>;
   constexpr size_t sp = plane_smem<T, NX, NY>();
   static bool attr = false;
@@ -895,10 +895,31 @@ static void chains_shape(const ChainJob<T>* jobs, int njobs, int maxsteps, int n
     return;
   }
   if constexpr (NY > 1) {
+    const double ng = (double)C::NP * nz;
+    if (br && br->n > 0 && njobs > 1) {
+      // one branch stream per job: chains of different lengths and phases overlap
+      cudaEventRecord(br->fork, st);
+      const int nb = br->n < njobs ? br->n : njobs;
+      for (int b = 0; b < nb; ++b) cudaStreamWaitEvent(br->s[b], br->fork, 0);
+      for (int j = 0; j < njobs; ++j) {
+        cudaStream_t sj = br->s[j % nb];
+        const int ns = br->steps[j];
+        for (int t = 0; t <= ns; ++t) {
+          xy_step_kernel<T, NX, NY><<<dim3(nz, 1), C::THREADS, sp, sj>>>(jobs + j, t, nz, tw);
+          count_launches(1);
+          if (t < ns) z_step_dispatch<T>(nz, jobs + j, t, C::NKP, ng, 1, tw, sj);
+        }
+      }
+      for (int b = 0; b < nb; ++b) {
+        cudaEventRecord(br->join[b], br->s[b]);
+        cudaStreamWaitEvent(st, br->join[b], 0);
+      }
+      return;
+    }
     for (int t = 0; t <= maxsteps; ++t) {
       xy_step_kernel<T, NX, NY><<<dim3(nz, njobs), C::THREADS, sp, st>>>(jobs, t, nz, tw);
       count_launches(1);
-      if (t < maxsteps) z_step_dispatch<T>(nz, jobs, t, C::NKP, (double)C::NP * nz, njobs, tw, st);
+      if (t < maxsteps) z_step_dispatch<T>(nz, jobs, t, C::NKP, ng, njobs, tw, st);
     }
   }
 }
@@ -992,11 +1013,11 @@ void launch_fill(T* a, T v, long n, cudaStream_t st) {
 
 template <typename T>
 void launch_chains(const ChainJob<T>* jobs_dev, int njobs, int maxsteps, const GridDims& d, const Twiddles<T>& tw,
-                   cudaStream_t st) {
+                   cudaStream_t st, const Branches* br) {
   switch (shape_key(d.nx, d.ny)) {
-#define PF_S(A, B)                                                   \
-  case A * 1024 + B:                                                 \
-    chains_shape<T, A, B>(jobs_dev, njobs, maxsteps, d.nz, tw, st);  \
+#define PF_S(A, B)                                                       \
+  case A * 1024 + B:                                                     \
+    chains_shape<T, A, B>(jobs_dev, njobs, maxsteps, d.nz, tw, st, br);  \
     break;
     PF_PLANE_SHAPES(PF_S)
 #undef PF_S
@@ -1027,7 +1048,7 @@ void launch_stress(const StressItem<T>* items, int nitems, const T* const* src_q
   template void launch_ld<T>(T*, const CellGeom&, double, double, long, cudaStream_t);                    \
   template void launch_fill<T>(T*, T, long, cudaStream_t);                                                \
   template void launch_chains<T>(const ChainJob<T>*, int, int, const GridDims&, const Twiddles<T>&,       \
-                                 cudaStream_t);                                                            \
+                                 cudaStream_t, const Branches*);                                                          \
   template void launch_stress<T>(const StressItem<T>*, int, const T* const*, const T* const*, Cx<T>* const*, \
                                  Cx<T>* const*, const GridDims&, const double*, int, double*,              \
                                  const Twiddles<T>&, cudaStream_t);
