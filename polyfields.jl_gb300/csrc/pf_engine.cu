@@ -400,6 +400,21 @@ struct System {
   bool use_branches = true;
   Branches br;
   std::vector<int> job_steps;
+  // host views of the jobs (TMA descriptors of the pencil pass): per precision
+  std::vector<ChainHost<float>> hosts_f;
+  std::vector<ChainHost<double>> hosts_d;
+  std::vector<std::vector<const float*>> lds_f;
+  std::vector<std::vector<const double*>> lds_d;
+  template <typename T>
+  std::vector<ChainHost<T>>& hosts_of() {
+    if constexpr (sizeof(T) == 4) return hosts_f;
+    else return hosts_d;
+  }
+  template <typename T>
+  std::vector<std::vector<const T*>>& lds_of() {
+    if constexpr (sizeof(T) == 4) return lds_f;
+    else return lds_d;
+  }
   bool jobs_dirty[2] = {true, true};
   bool timing = false;
   // density solves replay a captured CUDA graph per precision (PF_NO_GRAPHS=1 disables)
@@ -654,6 +669,10 @@ struct System {
     gexec[p] = nullptr;
     graph_warm[p] = false;
     std::vector<ChainJob<T>> hjobs;
+    auto& hosts = hosts_of<T>();
+    auto& lds = lds_of<T>();
+    hosts.clear();
+    lds.clear();
     maxsteps = 0;
     for (auto& spp : species) {
       Species& sp = *spp;
@@ -714,9 +733,21 @@ struct System {
       }
       hjobs.push_back(ChainJob<T>{sp.q[p].as<T>(), ops, kb0, c0, l0, 0, +1, sp.Ns, 0});
       if (nb > 1) hjobs.push_back(ChainJob<T>{sp.qc[p].as<T>(), ops + sp.Ns, kb1, c1, l1, sp.Ns, -1, sp.Ns, 0});
+      for (int dir = 0; dir < (nb > 1 ? 2 : 1); ++dir) {
+        std::vector<const T*> l(sp.Ns);
+        for (int t = 0; t < sp.Ns; ++t) l[t] = hops[(size_t)dir * sp.Ns + t].ld;
+        lds.push_back(std::move(l));
+        ChainHost<T> h;
+        h.kbuf = dir ? kb1 : kb0;
+        h.csc = dir ? c1 : c0;
+        h.lsc = dir ? l1 : l0;
+        h.nsteps = sp.Ns;
+        hosts.push_back(h);
+      }
       maxsteps = std::max(maxsteps, sp.Ns);
     }
     njobs = (int)hjobs.size();
+    for (size_t j = 0; j < hosts.size(); ++j) hosts[j].ld = lds[j].data();
     job_steps.clear();
     for (const auto& j : hjobs) job_steps.push_back(j.nsteps);
     jobs[p].alloc(sizeof(ChainJob<T>) * std::max(1, njobs));
@@ -749,7 +780,8 @@ struct System {
     }
     record_ev(1);
     if (njobs)
-      launch_chains<T>(jobs[p].as<ChainJob<T>>(), njobs, maxsteps, GridDims{nx, ny, nz}, tw<T>(p), st, branches());
+      launch_chains<T>(jobs[p].as<ChainJob<T>>(), njobs, maxsteps, GridDims{nx, ny, nz}, tw<T>(p), st,
+                       hosts_of<T>().data(), branches());
     record_ev(2);
     for (auto& spp : species) {
       Species& sp = *spp;
@@ -1296,7 +1328,12 @@ struct System {
     ChainJob<T> hj{hist.as<T>(), ops.as<StepOp<T>>(), kp, nullptr, nullptr, 0, +1, nsteps, 0};
     job.alloc(sizeof(hj));
     PF_CU(cudaMemcpyAsync(job.p, &hj, sizeof(hj), cudaMemcpyHostToDevice, st));
-    launch_chains<T>(job.as<ChainJob<T>>(), 1, nsteps, GridDims{nx, ny, nz}, tw<T>(p), st);
+    std::vector<const T*> ld_steps(nsteps, ld.as<T>());
+    ChainHost<T> host;
+    host.kbuf = kp;
+    host.nsteps = nsteps;
+    host.ld = ld_steps.data();
+    launch_chains<T>(job.as<ChainJob<T>>(), 1, nsteps, GridDims{nx, ny, nz}, tw<T>(p), st, &host);
     check_launch();
     std::vector<T> ho(ng);
     PF_CU(cudaMemcpyAsync(ho.data(), hist.as<T>() + (long)nsteps * ng, sizeof(T) * ng, cudaMemcpyDeviceToHost, st));

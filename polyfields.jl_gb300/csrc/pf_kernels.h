@@ -96,9 +96,23 @@ struct Branches {
   cudaEvent_t join[kMaxBranches] = {};
   const int* steps = nullptr;
 };
+// Host-side view of a chain job, for launchers that build TMA descriptors of its buffers.
+template <typename T>
+struct ChainHost {
+  Cx<T>* kbuf = nullptr;         // half-spectrum scratch, [kz][kx][ky]
+  float* csc = nullptr;          // per-step rescale factors (float32 chains), or null
+  double* lsc = nullptr;
+  int nsteps = 0;
+  const T* const* ld = nullptr;  // bond operator of each step (host array of nsteps pointers)
+};
+// 3D grids need hosts (njobs entries); 1D/2D grids ignore it.
 template <typename T>
 void launch_chains(const ChainJob<T>* jobs_dev, int njobs, int maxsteps, const GridDims& d, const Twiddles<T>& tw,
-                   cudaStream_t st, const Branches* br = nullptr);
+                   cudaStream_t st, const ChainHost<T>* hosts, const Branches* br = nullptr);
+// Nonzero when a pipelined kernel of this precision gave up waiting on a copy since the
+// last call (reads and clears a device flag; synchronises the stream).
+template <typename T>
+int take_pipe_status(cudaStream_t st);
 // Stress sums: Nz == 1 uses items (device array of nitems); 3D grids use the pointer arrays
 // src_q/src_qc (real grids) and kq/kqc (half-spectrum scratch), each nitems long.
 template <typename T>

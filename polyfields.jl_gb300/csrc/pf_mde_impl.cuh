@@ -29,6 +29,9 @@
 #pragma once
 #include "pf_fft.cuh"
 #include "pf_kernels.h"
+#include "pf_tma.cuh"
+#include <cudaTypedefs.h>
+#include <stdexcept>
 
 namespace pf {
 
@@ -650,6 +653,231 @@ __global__ void __launch_bounds__(512)
   }
 }
 
+// ------------------------------------------------------------------ 3D: pencil pass through TMA
+// The pencil pass as a pipeline: a tile is M pencils (M * sizeof(Cx<T>) = 128 bytes, one row
+// per z) brought into shared memory by one 2D TMA copy with the 128-byte swizzle, together with
+// the matching LD tile (64-byte rows, 64-byte swizzle).  The forward transform reads the rows
+// in natural order and works in place on the tile (intermediate passes in a permuted row order,
+// zrow_perm, that spreads each group's accesses over the banks under the swizzle); after LD and
+// the inverse transform the tile goes back to global memory with one TMA store.  Each CTA runs
+// several tiles through STAGES buffers, so copies of the next tiles overlap the transforms.
+static __device__ int g_pipe_status;  // nonzero: a pipeline wait gave up (the launch's output is invalid)
+
+template <typename T, int NZ>
+struct ZPipe {
+  static constexpr int E = (int)sizeof(Cx<T>);
+  static constexpr int M = 128 / E;              // pencils per tile
+  static constexpr int G = Plan<NZ>::G;
+  static constexpr int TT = M * G;               // threads per tile
+  static constexpr int TPC = TT >= 128 ? 1 : 128 / TT;  // tiles per stage
+  static constexpr int THREADS = TPC * TT;
+  static constexpr int KB = NZ * 128;            // bytes of a spectrum tile
+  static constexpr int LB = NZ * 64;             // bytes of an LD tile (M values of T per row)
+  static constexpr int STAGES = 2;
+  static constexpr int SMEM = STAGES * TPC * (KB + LB) + 1024;  // + alignment of the 1024-byte swizzle atom
+  // CTAs per SM that the shared memory allows (at most 4): the register budget follows from it
+  static constexpr int MINB = (200 * 1024 / SMEM) < 1 ? 1 : ((200 * 1024 / SMEM) > 4 ? 4 : (200 * 1024 / SMEM));
+  // group -> pencil stride (a bank-conflict count under the swizzle picked 5 for 4-thread groups)
+  static constexpr int PSTRIDE = G == 4 ? 5 : 1;
+};
+
+// Row order of the intermediate passes (a bijection on [0, NZ) that only permutes the low
+// three bits, i.e. the 16-byte chunk a row's element lands in under the 128-byte swizzle).
+template <int NZ>
+__device__ __forceinline__ int zrow_perm(int i) {
+  if constexpr (NZ == 128 || NZ == 96) return i ^ (((i >> 3) ^ (i >> 6)) & 7);
+  else if constexpr (NZ == 64 || NZ == 32) return i ^ ((i >> 3) & 7);
+  else if constexpr (NZ == 256) return swz(i);
+  else return i;
+}
+
+// Element (row z, pencil m) of a spectrum tile under the 128-byte swizzle: the 16-byte chunk
+// index of the 128-byte row is XORed with z mod 8 (the buffer is 1024-byte aligned).
+template <typename T>
+__device__ __forceinline__ int ktile_index(int z, int m) {
+  constexpr int E = (int)sizeof(Cx<T>);
+  const int b = m * E;
+  return (z * 128 + ((((b >> 4) ^ (z & 7)) << 4) | (b & 15))) / E;
+}
+// Element (row z, pencil m) of an LD tile under the 64-byte swizzle: the chunk index of the
+// 64-byte row is XORed with (z / 2) mod 4 (the buffer is 512-byte aligned).
+template <typename T>
+__device__ __forceinline__ int ltile_index(int z, int m) {
+  const int b = m * (int)sizeof(T);
+  return (z * 64 + ((((b >> 4) ^ ((z >> 1) & 3)) << 4) | (b & 15))) / (int)sizeof(T);
+}
+
+template <typename T, bool INV, int N, int O, int P0, int P1>
+__device__ __forceinline__ void ztile_passes(Cx<T>* kt, int m, int g, const Cx<T>* tw, bool active) {
+  if constexpr (P0 < P1) {
+    using PS = PassOf<T, INV, N, O, P0>;
+    Cx<T> v[PS::BPT][Order<N, O>::radix(P0)];
+    if (active) {
+      PS::load(v, g, [&](int i) { return kt[ktile_index<T>(zrow_perm<N>(i), m)]; });
+      PS::compute(v, g, tw + Order<N, O>::tw_offset(P0));
+    }
+    __syncwarp();
+    if (active) PS::store(v, g, [&](int i, const Cx<T>& x) { kt[ktile_index<T>(zrow_perm<N>(i), m)] = x; });
+    __syncwarp();
+    ztile_passes<T, INV, N, O, P0 + 1, P1>(kt, m, g, tw, active);
+  }
+}
+
+// Forward z transform (order B) of pencil m of a tile, ending in registers at the B -> A join.
+template <typename T, int NZ>
+__device__ __forceinline__ void ztile_forward(Cx<T>* kt, int m, int g, const Cx<T>* twb, BARegs<T, NZ>& w,
+                                              bool active) {
+  constexpr int P = Order<NZ, 1>::P;
+  using F0 = PassOf<T, false, NZ, 1, 0>;
+  if constexpr (P == 1) {
+    if (active) {
+      F0::load(w.v, g, [&](int i) { return kt[ktile_index<T>(i, m)]; });
+      F0::compute(w.v, g, twb);
+    }
+  } else {
+    Cx<T> v[F0::BPT][Order<NZ, 1>::radix(0)];
+    if (active) {
+      F0::load(v, g, [&](int i) { return kt[ktile_index<T>(i, m)]; });
+      F0::compute(v, g, twb);
+    }
+    __syncwarp();
+    if (active) F0::store(v, g, [&](int i, const Cx<T>& x) { kt[ktile_index<T>(zrow_perm<NZ>(i), m)] = x; });
+    __syncwarp();
+    ztile_passes<T, false, NZ, 1, 1, P - 1>(kt, m, g, twb, active);
+    using FL = PassOf<T, false, NZ, 1, P - 1>;
+    if (active) {
+      FL::load(w.v, g, [&](int i) { return kt[ktile_index<T>(zrow_perm<NZ>(i), m)]; });
+      FL::compute(w.v, g, twb + Order<NZ, 1>::tw_offset(P - 1));
+    }
+  }
+  __syncwarp();
+}
+
+// Inverse z transform (order A) from registers at the join back into the tile, natural rows.
+template <typename T, int NZ>
+__device__ __forceinline__ void ztile_inverse(Cx<T>* kt, int m, int g, const Cx<T>* twa, BARegs<T, NZ>& w,
+                                              bool active) {
+  constexpr int P = Order<NZ, 0>::P;
+  using I0 = PassOf<T, true, NZ, 0, 0>;
+  if constexpr (P == 1) {
+    if (active) {
+      I0::compute(w.v, g, twa);
+      I0::store(w.v, g, [&](int i, const Cx<T>& x) { kt[ktile_index<T>(i, m)] = x; });
+    }
+  } else {
+    if (active) {
+      I0::compute(w.v, g, twa);
+      I0::store(w.v, g, [&](int i, const Cx<T>& x) { kt[ktile_index<T>(zrow_perm<NZ>(i), m)] = x; });
+    }
+    __syncwarp();
+    ztile_passes<T, true, NZ, 0, 1, P - 1>(kt, m, g, twa, active);
+    using IL = PassOf<T, true, NZ, 0, P - 1>;
+    Cx<T> v[IL::BPT][Order<NZ, 0>::radix(P - 1)];
+    if (active) {
+      IL::load(v, g, [&](int i) { return kt[ktile_index<T>(zrow_perm<NZ>(i), m)]; });
+      IL::compute(v, g, twa + Order<NZ, 0>::tw_offset(P - 1));
+    }
+    __syncwarp();
+    if (active) IL::store(v, g, [&](int i, const Cx<T>& x) { kt[ktile_index<T>(i, m)] = x; });
+  }
+}
+
+// One contour step's pencil pass of one chain: forward z, LD (and, for tile 0, the rescale
+// factor of the step from the (0,0,0) coefficient), inverse z.  kmap views the chain's
+// half-spectrum scratch as rows of Nkp elements (8-byte units), lmap the step's LD.
+template <typename T, int NZ>
+__global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
+    z_pipe_kernel(const __grid_constant__ CUtensorMap kmap, const __grid_constant__ CUtensorMap lmap,
+                  float* __restrict__ csc, double* __restrict__ lsc, int t, int ntiles, double ng, Twiddles<T> twg) {
+  using Z = ZPipe<T, NZ>;
+  constexpr int S = Z::STAGES, TPC = Z::TPC, G = Z::G;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* sbase = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                          ~static_cast<uintptr_t>(1023));
+  Cx<T>* ktiles = reinterpret_cast<Cx<T>*>(sbase);                    // [S][TPC] tiles of KB bytes
+  T* ltiles = reinterpret_cast<T*>(sbase + (size_t)S * TPC * Z::KB);  // [S][TPC] tiles of LB bytes
+  __shared__ __align__(8) uint64_t full[S];
+  __shared__ Cx<T> twz[tw_total<NZ>()];
+  const int nrounds = (ntiles + TPC - 1) / TPC;
+  const int nk = (int)blockIdx.x < nrounds ? (nrounds - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  stage<T>(twz, twg.z, tw_total<NZ>());
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int k) {  // thread 0: fill stage k % S with round k of this CTA
+    const int s = k % S, r = (int)blockIdx.x + k * (int)gridDim.x;
+    const int nt = min(TPC, ntiles - r * TPC);
+    mbar_expect_tx(&full[s], (unsigned)(nt * (Z::KB + Z::LB)));
+    for (int j = 0; j < nt; ++j) {
+      const int tile = r * TPC + j;
+      tma_load_2d(ktiles + (size_t)(s * TPC + j) * (Z::KB / Z::E), &kmap, tile * 16, 0, &full[s]);
+      tma_load_2d(ltiles + (size_t)(s * TPC + j) * (Z::LB / sizeof(T)), &lmap, tile * Z::M, 0, &full[s]);
+    }
+  };
+  if (threadIdx.x == 0)
+    for (int k = 0; k < S - 1 && k < nk; ++k) issue(k);
+  const int slot = threadIdx.x / Z::TT, lt = threadIdx.x % Z::TT;
+  const int m = ((lt / G) * Z::PSTRIDE) % Z::M, g = lt % G;
+  const Cx<T>* twb = twz + Order<NZ, 0>::TW_SIZE;
+  int waited = 0;  // rounds whose stage completed
+  bool ok = true;
+#pragma unroll 1
+  for (int k = 0; k < nk; ++k) {
+    const int s = k % S, r = (int)blockIdx.x + k * (int)gridDim.x;
+    const bool good = mbar_wait(&full[s], (unsigned)((k / S) & 1));
+    if (__syncthreads_or(!good)) {
+      ok = false;
+      break;
+    }
+    waited = k + 1;
+    const int tile = r * TPC + slot;
+    const bool active = tile < ntiles;
+    Cx<T>* kt = ktiles + (size_t)(s * TPC + slot) * (Z::KB / Z::E);
+    const T* ltl = ltiles + (size_t)(s * TPC + slot) * (Z::LB / sizeof(T));
+    BARegs<T, NZ> w;
+    ztile_forward<T, NZ>(kt, m, g, twb, w, active);
+    if (csc && r == 0 && threadIdx.x == 0) {
+      // tile 0, pencil 0, position 0: the (0, 0, 0) coefficient = grid sum of LW * q_t
+      const T c = rescale_factor<T>(w.v[0][0].x, ng);
+      csc[t] = (float)c;
+      lsc[t] = log((double)c);
+    }
+    if (active) {
+#pragma unroll
+      for (int b = 0; b < JoinBA<NZ>::BPT; ++b)
+#pragma unroll
+        for (int tt = 0; tt < JoinBA<NZ>::R; ++tt) {
+          const T f = ltl[ltile_index<T>(JoinBA<NZ>::pos(g, b, tt), m)];
+          w.v[b][tt] = cx<T>(w.v[b][tt].x * f, w.v[b][tt].y * f);
+        }
+    }
+    ztile_inverse<T, NZ>(kt, m, g, twz, w, active);
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int nt = min(TPC, ntiles - r * TPC);
+      for (int j = 0; j < nt; ++j)
+        tma_store_2d(&kmap, (r * TPC + j) * 16, 0, ktiles + (size_t)(s * TPC + j) * (Z::KB / Z::E));
+      bulk_commit();
+      if (k + S - 1 < nk) {
+        bulk_wait_read<1>();  // the store of round k-1 has left stage (k-1) % S
+        issue(k + S - 1);
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    bulk_wait<0>();
+    if (!ok) {
+      g_pipe_status = 1;
+      // drain the copies still in flight into this CTA's stages (bounded waits)
+      const int issued = min(nk, waited + S - 1);
+      for (int k = waited; k < issued; ++k) mbar_wait(&full[k % S], (unsigned)((k / S) & 1));
+    }
+  }
+}
+
 // ------------------------------------------------------------------ stress transforms
 // Sum over the half spectrum of c_k Re(qhat_k) Re(qchat_k) dksq_p,k with c_0 = 1 and c_k = 2
 // otherwise (quirk Q2, multiblock.jl:279-282), for every item (a contour point of a block).
@@ -878,9 +1106,105 @@ static bool z_step_dispatch(int nz, const ChainJob<T>* jobs, int t, int nkp, dou
   }
 }
 
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime.
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// TMA views of a chain's half-spectrum scratch (rows of Nkp complex values, one per kz, as
+// 8-byte units; boxes of 128 bytes x Nz rows, 128-byte swizzle) and of an LD array (rows of
+// Nkp values of T; boxes of 64 bytes x Nz rows, 64-byte swizzle).
+template <typename T>
+static void make_zmaps(CUtensorMap* km, CUtensorMap* lm, const Cx<T>* kbuf, const T* ld, int nkp, int nz) {
+  auto enc = tmap_encoder();
+  if (!enc) throw std::runtime_error("cuTensorMapEncodeTiled is not available from the driver");
+  // box starts are multiples of 128 (scratch) and 64 (LD) bytes; rows must be 16-byte strided
+  if (nkp % 4 != 0 || nz > 256 || (reinterpret_cast<uintptr_t>(kbuf) & 15) || (reinterpret_cast<uintptr_t>(ld) & 15))
+    throw std::runtime_error("pencil pass: spectrum rows or buffers not 16-byte aligned");
+  const cuuint32_t es[2] = {1, 1};
+  {
+    const cuuint64_t dim[2] = {(cuuint64_t)nkp * (sizeof(Cx<T>) / 8), (cuuint64_t)nz};
+    const cuuint64_t str[1] = {(cuuint64_t)nkp * sizeof(Cx<T>)};
+    const cuuint32_t box[2] = {16, (cuuint32_t)nz};
+    if (enc(km, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<Cx<T>*>(kbuf), dim, str, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      throw std::runtime_error("cuTensorMapEncodeTiled failed for a half-spectrum scratch");
+  }
+  {
+    const cuuint64_t dim[2] = {(cuuint64_t)nkp, (cuuint64_t)nz};
+    const cuuint64_t str[1] = {(cuuint64_t)nkp * sizeof(T)};
+    const cuuint32_t box[2] = {(cuuint32_t)(64 / sizeof(T)), (cuuint32_t)nz};
+    if (enc(lm, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2,
+            const_cast<T*>(ld), dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      throw std::runtime_error("cuTensorMapEncodeTiled failed for a bond operator");
+  }
+}
+
+// rounds (stages of tiles) per CTA of the pencil pipeline
+constexpr int kZRoundsPerCta = 2;
+
+template <typename T, int NZ>
+static void launch_z_pipe(const ChainHost<T>& h, int t, int nkp, double ng, const Twiddles<T>& tw,
+                          cudaStream_t st) {
+  using Z = ZPipe<T, NZ>;
+  static int grid_cap = 0;
+  if (!grid_cap) {
+    set_smem(z_pipe_kernel<T, NZ>, Z::SMEM);
+    int occ = 0, dev = 0, nsm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, z_pipe_kernel<T, NZ>, Z::THREADS, Z::SMEM);
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    grid_cap = (occ > 0 ? occ : 1) * (nsm > 0 ? nsm : 1);
+  }
+  CUtensorMap km, lm;
+  make_zmaps<T>(&km, &lm, h.kbuf, h.ld[t], nkp, NZ);
+  const int ntiles = (nkp + Z::M - 1) / Z::M;
+  const int nrounds = (ntiles + Z::TPC - 1) / Z::TPC;
+  int grid = (nrounds + kZRoundsPerCta - 1) / kZRoundsPerCta;
+  if (grid > grid_cap) grid = grid_cap;
+  if (grid < 1) grid = 1;
+  z_pipe_kernel<T, NZ><<<grid, Z::THREADS, Z::SMEM, st>>>(km, lm, h.csc, h.lsc, t, ntiles, ng, tw);
+  count_launches(1);
+}
+
+template <typename T>
+static void z_pipe_dispatch(int nz, const ChainHost<T>& h, int t, int nkp, double ng, const Twiddles<T>& tw,
+                            cudaStream_t st) {
+  switch (nz) {
+#define PF_Z(N)                                        \
+  case N:                                              \
+    launch_z_pipe<T, N>(h, t, nkp, ng, tw, st);        \
+    return;
+    PF_Z_LENGTHS(PF_Z)
+#undef PF_Z
+    default:
+      return;
+  }
+}
+
+template <typename T>
+int take_pipe_status(cudaStream_t st) {
+  int v = 0;
+  const int zero = 0;
+  cudaMemcpyFromSymbolAsync(&v, g_pipe_status, sizeof(int), 0, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyToSymbolAsync(g_pipe_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+  cudaStreamSynchronize(st);
+  return v;
+}
+
 template <typename T, int NX, int NY>
 static void chains_shape(const ChainJob<T>* jobs, int njobs, int maxsteps, int nz, const Twiddles<T>& tw,
-                         cudaStream_t st, const Branches* br) {
+                         cudaStream_t st, const ChainHost<T>* hosts, const Branches* br) {
   using C = PlaneCfg<NX, NY>;
   constexpr size_t sp = plane_smem<T, NX, NY>();
   static bool attr = false;
@@ -895,32 +1219,30 @@ static void chains_shape(const ChainJob<T>* jobs, int njobs, int maxsteps, int n
     return;
   }
   if constexpr (NY > 1) {
+    if (!hosts) throw std::runtime_error("3D chains need the jobs' host descriptions");
     const double ng = (double)C::NP * nz;
+    // job j's steps on stream sj: plane pass t (finishing t-1, starting t), pencil pass t
+    auto run_job = [&](int j, cudaStream_t sj) {
+      const int ns = hosts[j].nsteps;
+      for (int t = 0; t <= ns; ++t) {
+        xy_step_kernel<T, NX, NY><<<dim3(nz, 1), C::THREADS, sp, sj>>>(jobs + j, t, nz, tw);
+        count_launches(1);
+        if (t < ns) z_pipe_dispatch<T>(nz, hosts[j], t, C::NKP, ng, tw, sj);
+      }
+    };
     if (br && br->n > 0 && njobs > 1) {
       // one branch stream per job: chains of different lengths and phases overlap
       cudaEventRecord(br->fork, st);
       const int nb = br->n < njobs ? br->n : njobs;
       for (int b = 0; b < nb; ++b) cudaStreamWaitEvent(br->s[b], br->fork, 0);
-      for (int j = 0; j < njobs; ++j) {
-        cudaStream_t sj = br->s[j % nb];
-        const int ns = br->steps[j];
-        for (int t = 0; t <= ns; ++t) {
-          xy_step_kernel<T, NX, NY><<<dim3(nz, 1), C::THREADS, sp, sj>>>(jobs + j, t, nz, tw);
-          count_launches(1);
-          if (t < ns) z_step_dispatch<T>(nz, jobs + j, t, C::NKP, ng, 1, tw, sj);
-        }
-      }
+      for (int j = 0; j < njobs; ++j) run_job(j, br->s[j % nb]);
       for (int b = 0; b < nb; ++b) {
         cudaEventRecord(br->join[b], br->s[b]);
         cudaStreamWaitEvent(st, br->join[b], 0);
       }
       return;
     }
-    for (int t = 0; t <= maxsteps; ++t) {
-      xy_step_kernel<T, NX, NY><<<dim3(nz, njobs), C::THREADS, sp, st>>>(jobs, t, nz, tw);
-      count_launches(1);
-      if (t < maxsteps) z_step_dispatch<T>(nz, jobs, t, C::NKP, ng, njobs, tw, st);
-    }
+    for (int j = 0; j < njobs; ++j) run_job(j, st);
   }
 }
 
@@ -1013,11 +1335,11 @@ void launch_fill(T* a, T v, long n, cudaStream_t st) {
 
 template <typename T>
 void launch_chains(const ChainJob<T>* jobs_dev, int njobs, int maxsteps, const GridDims& d, const Twiddles<T>& tw,
-                   cudaStream_t st, const Branches* br) {
+                   cudaStream_t st, const ChainHost<T>* hosts, const Branches* br) {
   switch (shape_key(d.nx, d.ny)) {
-#define PF_S(A, B)                                                       \
-  case A * 1024 + B:                                                     \
-    chains_shape<T, A, B>(jobs_dev, njobs, maxsteps, d.nz, tw, st, br);  \
+#define PF_S(A, B)                                                              \
+  case A * 1024 + B:                                                            \
+    chains_shape<T, A, B>(jobs_dev, njobs, maxsteps, d.nz, tw, st, hosts, br);  \
     break;
     PF_PLANE_SHAPES(PF_S)
 #undef PF_S
@@ -1048,7 +1370,8 @@ void launch_stress(const StressItem<T>* items, int nitems, const T* const* src_q
   template void launch_ld<T>(T*, const CellGeom&, double, double, long, cudaStream_t);                    \
   template void launch_fill<T>(T*, T, long, cudaStream_t);                                                \
   template void launch_chains<T>(const ChainJob<T>*, int, int, const GridDims&, const Twiddles<T>&,       \
-                                 cudaStream_t, const Branches*);                                                          \
+                                 cudaStream_t, const ChainHost<T>*, const Branches*);                     \
+  template int take_pipe_status<T>(cudaStream_t);                                                          \
   template void launch_stress<T>(const StressItem<T>*, int, const T* const*, const T* const*, Cx<T>* const*, \
                                  Cx<T>* const*, const GridDims&, const double*, int, double*,              \
                                  const Twiddles<T>&, cudaStream_t);

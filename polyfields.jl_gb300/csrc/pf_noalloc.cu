@@ -96,7 +96,18 @@ int propagate_noalloc(int nx, int ny, int nz, T* hist, const T* lw, const T* ld,
       cudaMemcpyAsync(tw_dev, htw.data(), sizeof(Cx<T>) * htw.size(), cudaMemcpyHostToDevice, st) != cudaSuccess)
     return E_CUDA;
   const Twiddles<T> tw{tw_dev + off[0], tw_dev + off[1], tw_dev + off[2]};
-  launch_chains<T>(job_dev, 1, nsteps, GridDims{nx, ny, nz}, tw, st);
+  // host view for the TMA descriptors of the pencil pass (host memory only)
+  std::vector<const T*> ld_steps(nsteps, ld);
+  ChainHost<T> host;
+  host.kbuf = kbuf;
+  host.nsteps = nsteps;
+  host.ld = ld_steps.data();
+  try {
+    launch_chains<T>(job_dev, 1, nsteps, GridDims{nx, ny, nz}, tw, st, &host);
+  } catch (const std::exception& e) {
+    fprintf(stderr, "pf_propagate_noalloc: %s\n", e.what());
+    return E_ARG;
+  }
   return cudaGetLastError() == cudaSuccess ? OK : E_CUDA;
 }
 
