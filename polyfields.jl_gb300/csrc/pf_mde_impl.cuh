@@ -673,10 +673,17 @@ struct ZPipe {
   static constexpr int THREADS = TPC * TT;
   static constexpr int KB = NZ * 128;            // bytes of a spectrum tile
   static constexpr int LB = NZ * 64;             // bytes of an LD tile (M values of T per row)
-  static constexpr int STAGES = 2;
+#ifndef PF_ZSTAGES
+#define PF_ZSTAGES 2
+#endif
+  static constexpr int STAGES = PF_ZSTAGES;
   static constexpr int SMEM = STAGES * TPC * (KB + LB) + 1024;  // + alignment of the 1024-byte swizzle atom
   // CTAs per SM that the shared memory allows (at most 4): the register budget follows from it
-  static constexpr int MINB = (200 * 1024 / SMEM) < 1 ? 1 : ((200 * 1024 / SMEM) > 4 ? 4 : (200 * 1024 / SMEM));
+#ifndef PF_ZMINB
+#define PF_ZMINB 3
+#endif
+  static constexpr int MINB =
+      (200 * 1024 / SMEM) < 1 ? 1 : ((200 * 1024 / SMEM) > PF_ZMINB ? PF_ZMINB : (200 * 1024 / SMEM));
   // group -> pencil stride (a bank-conflict count under the swizzle picked 5 for 4-thread groups)
   static constexpr int PSTRIDE = G == 4 ? 5 : 1;
 };
@@ -1151,7 +1158,10 @@ static void make_zmaps(CUtensorMap* km, CUtensorMap* lm, const Cx<T>* kbuf, cons
 }
 
 // rounds (stages of tiles) per CTA of the pencil pipeline
-constexpr int kZRoundsPerCta = 2;
+#ifndef PF_ZRPC
+#define PF_ZRPC 2
+#endif
+constexpr int kZRoundsPerCta = PF_ZRPC;
 
 template <typename T, int NZ>
 static void launch_z_pipe(const ChainHost<T>& h, int t, int nkp, double ng, const Twiddles<T>& tw,
