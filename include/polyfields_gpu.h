@@ -145,6 +145,16 @@ int pf_domain_stress_error(pf_system* sys, double* out);
  * by pf_anderson_create (required) and pf_domain_create (used when use_domain != 0). */
 int pf_scft(pf_system* sys, const pf_scft_options* opts, int use_domain, pf_scft_results* out);
 
+/* Many independent scft! runs (a phase-diagram sweep: src/simulate.jl:60-148 once per
+ * FieldSystem) driven together: nthreads host threads (0: min(n, 32)) take the systems in
+ * decreasing order of cost (grid points x contour steps) and run pf_scft on each, every
+ * system on its own CUDA stream with its density solves replayed as CUDA graphs, so the GPU
+ * runs up to nthreads solves at once.  results[i] and status[i] receive system i's outcome
+ * (pf_last_error(systems[i]) its message); returns PF_OK when every run returned PF_OK, else
+ * the first nonzero status in index order.  A handle must not be used elsewhere meanwhile. */
+int pf_scft_batch(pf_system* const* systems, int n, const pf_scft_options* opts, int use_domain,
+                  pf_scft_results* results, int* status, int nthreads);
+
 /* ---- low level: PseudoSpectralSolver update! + propagate! (src/system/mde.jl:43-81) ----
  * Propagates nsteps RK2 steps from qin with the operators of (omega, vol, b, ds) on the
  * handle's current cell; qout receives the last step.  Host arrays. */

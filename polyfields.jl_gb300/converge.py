@@ -1,0 +1,64 @@
+"""Time-to-solution of the large-blend system: plain FP64 solve vs FP32 iterations with FP64 polish.
+
+    python polyfields.jl_gb300/converge.py [--n 128] [--nsteps 4000] [--switch 1e-5] [--modes fp64,mixed]
+
+Builds the large blend (AB diblock N100 fA0.4 at phi 0.8 + A homopolymer N50 at phi 0.2,
+chi 0.2, Ns 200, cubic cell L0 = 14, double-gyroid start plus 0.05 seeded noise) on an n^3
+grid and runs scft! with AndersonUpdater(nhist = 20) and DomainUpdater(nskip = 5, nper = 20)
+to ftol = stol = 1e-8, once with float64 propagators throughout and once with float32
+propagators until ferr < --switch followed by float64 iterations (the mixed path).  Prints
+one JSON line: wall time, iterations, final ferr/serr/fhelm and cell of each run, and the
+differences of the mixed run from the FP64 run (|dfhelm|, |dL|/L).
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import polyfields as pf  # noqa: E402
+from polyfields import workloads as W  # noqa: E402
+
+
+def run(n, precision, nsteps, switch, ftol, stol, nsout):
+    sysm = W.blend3d_system(pf, n=n, precision=precision)
+    sysm.synchronize()
+    opts = pf.SCFTOptions(nsteps=nsteps, ftol=ftol, stol=stol, nsout=nsout,
+                          mixed_switch_ferr=switch if precision == "fp32" else 0.0)
+    t0 = time.perf_counter()
+    r = pf.scft(sysm, pf.AndersonUpdater(nhist=20), domain=pf.DomainUpdater(nskip=5, nper=20), opts=opts)
+    sysm.synchronize()
+    wall = time.perf_counter() - t0
+    return {"precision": "mixed" if precision == "fp32" else "fp64", "wall_s": wall, "iterations": r.nsteps,
+            "converged": r.converged, "switch_step": r.switch_step, "ferr": r.ferr, "serr": r.serr,
+            "fhelm": r.fhelm, "L": float(sysm.cell.params[0])}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--nsteps", type=int, default=4000)
+    ap.add_argument("--switch", type=float, default=1e-5)
+    ap.add_argument("--ftol", type=float, default=1e-8)
+    ap.add_argument("--stol", type=float, default=1e-8)
+    ap.add_argument("--modes", default="mixed,fp64")
+    ap.add_argument("--nsout", type=int, default=0)
+    a = ap.parse_args()
+    out = {"workload": f"large blend {a.n}^3, Ns 200, nhist 20, nskip 5, nper 20", "ftol": a.ftol, "stol": a.stol,
+           "switch_ferr": a.switch, "runs": []}
+    for mode in a.modes.split(","):
+        prec = "fp32" if mode == "mixed" else "fp64"
+        out["runs"].append(run(a.n, prec, a.nsteps, a.switch, a.ftol, a.stol, a.nsout))
+        print(json.dumps(out["runs"][-1]), file=sys.stderr, flush=True)
+    runs = {r["precision"]: r for r in out["runs"]}
+    if "mixed" in runs and "fp64" in runs:
+        m, d = runs["mixed"], runs["fp64"]
+        out["abs_dfhelm"] = abs(m["fhelm"] - d["fhelm"])
+        out["rel_dL"] = abs(m["L"] - d["L"]) / abs(d["L"])
+        out["wall_speedup"] = d["wall_s"] / m["wall_s"]
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -7,6 +7,8 @@
 // scft! driver loop (src/simulate.jl:60-148).  The orchestration runs on the host; every
 // grid-sized operation runs on the device, on the handle's own stream.
 #include <cmath>
+#include <atomic>
+#include <thread>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -892,6 +894,21 @@ struct System {
     else density_t<float>(1);
   }
 
+  // relative cost of one density solve: grid points x contour steps of all chains
+  double solve_cost() const {
+    double steps = 0.0;
+    for (const auto& sp : species)
+      if (sp->kind == 0) steps += (double)sp->Ns * (sp->nblocks() > 1 ? 2 : 1);
+    return (double)ng * std::max(1.0, steps);
+  }
+  // A pencil-pass pipeline that gave up waiting on a TMA copy leaves a device flag.
+  void check_pipe(int p) {
+    if (nz == 1) return;
+    const int ps = p == 1 ? take_pipe_status<float>(st) : take_pipe_status<double>(st);
+    if (ps)
+      throw PFError(E_CUDA, "pencil pass: a TMA copy did not complete within its time limit; the last density "
+                            "solve is invalid");
+  }
   void fetch_Q() {
     for (auto& sp : species) {
       if (!sp->Q_valid) {
@@ -899,6 +916,7 @@ struct System {
       }
     }
     PF_CU(cudaStreamSynchronize(st));
+    check_pipe(last_prec);
     for (auto& sp : species) {
       sp->Q_valid = true;
       sp->mu = std::log(sp->phi / sp->Q);  // muphi! canonical (system.jl:248-259)
@@ -1338,6 +1356,7 @@ struct System {
     std::vector<T> ho(ng);
     PF_CU(cudaMemcpyAsync(ho.data(), hist.as<T>() + (long)nsteps * ng, sizeof(T) * ng, cudaMemcpyDeviceToHost, st));
     PF_CU(cudaStreamSynchronize(st));
+    check_pipe(p);
     for (long i = 0; i < ng; ++i) qout[i] = (double)ho[i];
   }
 };
@@ -1635,6 +1654,41 @@ int pf_scft(pf_system* sys, const pf_scft_options* opts, int use_domain, pf_scft
     if (!opts || !out) throw pf::PFError(PF_EARG, "null options/results");
     *out = s.scft(*opts, use_domain != 0);
   });
+}
+
+int pf_scft_batch(pf_system* const* systems, int n, const pf_scft_options* opts, int use_domain,
+                  pf_scft_results* results, int* status, int nthreads) {
+  if (!systems || n < 0 || !opts || !results || !status) return PF_EARG;
+  for (int i = 0; i < n; ++i)
+    if (!systems[i] || !systems[i]->s) return PF_EARG;
+  // longest runs first (grid points x contour steps per density solve), so the tail is short
+  std::vector<int> order(n);
+  std::vector<double> cost(n);
+  for (int i = 0; i < n; ++i) {
+    order[i] = i;
+    cost[i] = systems[i]->s->solve_cost();
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  const int nt = std::max(1, std::min(n, nthreads > 0 ? nthreads : 32));
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    cudaSetDevice(dev);
+    for (;;) {
+      const int k = next.fetch_add(1);
+      if (k >= n) break;
+      const int i = order[k];
+      status[i] = pf_scft(systems[i], opts, use_domain, &results[i]);
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+  worker();
+  for (auto& th : pool) th.join();
+  for (int i = 0; i < n; ++i)
+    if (status[i] != PF_OK) return status[i];
+  return PF_OK;
 }
 
 int pf_propagate(pf_system* sys, const double* omega, double vol, double b, double ds, const double* qin, double* qout,

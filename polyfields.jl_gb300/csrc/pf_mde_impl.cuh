@@ -20,9 +20,9 @@
 //
 // Grids with Nz == 1 (1D and 2D systems): one persistent CTA per chain runs all contour
 // steps (chain_plane_kernel).  3D grids: each step is a plane pass (xy_step_kernel, one CTA
-// per z plane) and a pencil pass (z_step_kernel, one CTA per 16 or 8 pencils); the plane
-// pass of step t fuses the end of step t-1 with the start of step t.  Independent chains
-// (forward q, backward qc, other species) advance together in the same launches.
+// per z plane) and a pencil pass (z_pipe_kernel, tiles of 16 or 8 pencils staged by TMA); the
+// plane pass of step t fuses the end of step t-1 with the start of step t.  Independent
+// chains (forward q, backward qc, other species) run on their own streams and overlap.
 //
 // Every kernel is specialised on its transform lengths at compile time; the host picks the
 // instantiation from the supported plane shapes below.
@@ -565,94 +565,6 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
   }
 }
 
-// ------------------------------------------------------------------ 3D: pencil pass
-// Forward z transform (order B) from global, LD (+ the rescale factor of tile 0) in
-// registers, inverse z transform (order A) back to global.  M consecutive pencils per CTA,
-// one group of G threads per pencil; the pencil tile in shared memory is pencil-major with
-// rows padded by one element.
-template <typename T, int NZ>
-__global__ void __launch_bounds__(512)
-    z_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nkp, double ng, Twiddles<T> twg) {
-  constexpr int M = ZCfg<T>::M;
-  constexpr int LDT = NZ + pencil_pad<NZ>();
-  constexpr int G = Plan<NZ>::G;
-  constexpr int P = Order<NZ, 0>::P;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  Cx<T>* Tl = reinterpret_cast<Cx<T>*>(smem_raw);
-  const ChainJob<T> job = jobs[blockIdx.y];
-  if (t >= job.nsteps) return;
-  __shared__ Cx<T> twz[tw_total<NZ>()];
-  stage<T>(twz, twg.z, tw_total<NZ>());
-  __syncthreads();
-  const Cx<T>* twb = twz + Order<NZ, 0>::TW_SIZE;
-  const int m0 = blockIdx.x * M;
-  const int mm = threadIdx.x / G, g = threadIdx.x % G;
-  const bool active = mm < M && m0 + mm < nkp;
-  const long col = m0 + (active ? mm : 0);
-  Cx<T>* pen = Tl + (active ? mm : 0) * LDT;
-  Cx<T>* kb = job.kbuf;
-  BARegs<T, NZ> w;
-  using F0 = PassOf<T, false, NZ, 1, 0>;
-  if constexpr (P == 1) {
-    if (active) {
-      F0::load(w.v, g, [&](int i) { return kb[(long)i * nkp + col]; });
-      F0::compute(w.v, g, twb);
-    }
-  } else {
-    Cx<T> v[F0::BPT][Order<NZ, 1>::radix(0)];
-    if (active) {
-      F0::load(v, g, [&](int i) { return kb[(long)i * nkp + col]; });
-      F0::compute(v, g, twb);
-      F0::store(v, g, [&](int i, const Cx<T>& x) { pen[swz(i)] = x; });
-    }
-    __syncwarp();
-    smem_passes<T, false, NZ, 1, 1, P - 1, true, true>(pen, 1, g, twb, active);
-    using FL = PassOf<T, false, NZ, 1, P - 1>;
-    if (active) {
-      FL::load(w.v, g, [&](int i) { return pen[swz(i)]; });
-      FL::compute(w.v, g, twb + Order<NZ, 1>::tw_offset(P - 1));
-    }
-    __syncwarp();
-  }
-  if (job.csc && blockIdx.x == 0 && threadIdx.x == 0) {
-    // pencil 0, position 0: the (0, 0, 0) coefficient = grid sum of LW * q_t
-    const T c = rescale_factor<T>(w.v[0][0].x, ng);
-    job.csc[t] = (float)c;
-    job.lsc[t] = log((double)c);
-  }
-  if (active) {
-    const T* ld = job.ops[t].ld;
-#pragma unroll
-    for (int b = 0; b < JoinBA<NZ>::BPT; ++b)
-#pragma unroll
-      for (int tt = 0; tt < JoinBA<NZ>::R; ++tt) {
-        const T f = ld[(long)JoinBA<NZ>::pos(g, b, tt) * nkp + col];
-        w.v[b][tt] = cx<T>(w.v[b][tt].x * f, w.v[b][tt].y * f);
-      }
-  }
-  using I0 = PassOf<T, true, NZ, 0, 0>;
-  if constexpr (P == 1) {
-    if (active) {
-      I0::compute(w.v, g, twz);
-      I0::store(w.v, g, [&](int i, const Cx<T>& x) { kb[(long)i * nkp + col] = x; });
-    }
-  } else {
-    if (active) {
-      I0::compute(w.v, g, twz);
-      I0::store(w.v, g, [&](int i, const Cx<T>& x) { pen[swz(i)] = x; });
-    }
-    __syncwarp();
-    smem_passes<T, true, NZ, 0, 1, P - 1, true, true>(pen, 1, g, twz, active);
-    using IL = PassOf<T, true, NZ, 0, P - 1>;
-    Cx<T> v[IL::BPT][Order<NZ, 0>::radix(P - 1)];
-    if (active) {
-      IL::load(v, g, [&](int i) { return pen[swz(i)]; });
-      IL::compute(v, g, twz + Order<NZ, 0>::tw_offset(P - 1));
-      IL::store(v, g, [&](int i, const Cx<T>& x) { kb[(long)i * nkp + col] = x; });
-    }
-  }
-}
-
 // ------------------------------------------------------------------ 3D: pencil pass through TMA
 // The pencil pass as a pipeline: a tile is M pencils (M * sizeof(Cx<T>) = 128 bytes, one row
 // per z) brought into shared memory by one 2D TMA copy with the 128-byte swizzle, together with
@@ -1083,36 +995,6 @@ static constexpr int z_threads() {
   return round32(ZCfg<T>::M * Plan<NZ>::G);
 }
 
-template <typename T, int NZ>
-static void launch_z_step(const ChainJob<T>* jobs, int t, int nkp, double ng, int njobs, const Twiddles<T>& tw,
-                          cudaStream_t st) {
-  constexpr int M = ZCfg<T>::M;
-  const size_t sz = sizeof(Cx<T>) * (size_t)(NZ + pencil_pad<NZ>()) * M;
-  static bool attr = false;
-  if (!attr) {
-    set_smem(z_step_kernel<T, NZ>, sz);
-    attr = true;
-  }
-  const int ntiles = (nkp + M - 1) / M;
-  z_step_kernel<T, NZ><<<dim3(ntiles, njobs), z_threads<T, NZ>(), sz, st>>>(jobs, t, nkp, ng, tw);
-  count_launches(1);
-}
-
-template <typename T>
-static bool z_step_dispatch(int nz, const ChainJob<T>* jobs, int t, int nkp, double ng, int njobs,
-                            const Twiddles<T>& tw, cudaStream_t st) {
-  switch (nz) {
-#define PF_Z(N)                                           \
-  case N:                                                 \
-    launch_z_step<T, N>(jobs, t, nkp, ng, njobs, tw, st); \
-    return true;
-    PF_Z_LENGTHS(PF_Z)
-#undef PF_Z
-    default:
-      return false;
-  }
-}
-
 // cuTensorMapEncodeTiled from the driver, looked up once through the runtime.
 static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
@@ -1167,15 +1049,14 @@ template <typename T, int NZ>
 static void launch_z_pipe(const ChainHost<T>& h, int t, int nkp, double ng, const Twiddles<T>& tw,
                           cudaStream_t st) {
   using Z = ZPipe<T, NZ>;
-  static int grid_cap = 0;
-  if (!grid_cap) {
+  static const int grid_cap = [] {  // thread-safe one-time setup
     set_smem(z_pipe_kernel<T, NZ>, Z::SMEM);
     int occ = 0, dev = 0, nsm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, z_pipe_kernel<T, NZ>, Z::THREADS, Z::SMEM);
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    grid_cap = (occ > 0 ? occ : 1) * (nsm > 0 ? nsm : 1);
-  }
+    return (occ > 0 ? occ : 1) * (nsm > 0 ? nsm : 1);
+  }();
   CUtensorMap km, lm;
   make_zmaps<T>(&km, &lm, h.kbuf, h.ld[t], nkp, NZ);
   const int ntiles = (nkp + Z::M - 1) / Z::M;
@@ -1217,12 +1098,12 @@ static void chains_shape(const ChainJob<T>* jobs, int njobs, int maxsteps, int n
                          cudaStream_t st, const ChainHost<T>* hosts, const Branches* br) {
   using C = PlaneCfg<NX, NY>;
   constexpr size_t sp = plane_smem<T, NX, NY>();
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [] {  // thread-safe one-time setup
     set_smem(chain_plane_kernel<T, NX, NY>, sp);
     if constexpr (NY > 1) set_smem(xy_step_kernel<T, NX, NY>, sp);
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   if (nz == 1) {
     chain_plane_kernel<T, NX, NY><<<njobs, C::THREADS, sp, st>>>(jobs, tw);
     count_launches(1);
@@ -1263,12 +1144,12 @@ static void stress_shape(const StressItem<T>* items, int nitems, const T* const*
   using C = PlaneCfg<NX, NY>;
   constexpr size_t sp = plane_smem<T, NX, NY>();
   constexpr size_t ss = sp + sizeof(T) * (size_t)C::NKP;
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [] {  // thread-safe one-time setup
     set_smem(stress_plane_kernel<T, NX, NY>, ss);
     if constexpr (NY > 1) set_smem(xy_fwd_kernel<T, NX, NY>, sp);
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   if (nz == 1) {
     stress_plane_kernel<T, NX, NY><<<nitems, C::THREADS, ss, st>>>(items, dksq, nparams, part, tw);
     count_launches(1);
@@ -1285,11 +1166,8 @@ static void stress_shape(const StressItem<T>* items, int nitems, const T* const*
 #define PF_Z(N)                                                                                                    \
   case N: {                                                                                                        \
     const size_t sz = 2 * sizeof(Cx<T>) * (size_t)(N + pencil_pad<N>()) * M;                                       \
-    static bool za = false;                                                                                        \
-    if (!za) {                                                                                                     \
-      set_smem(z_fwd_stress_kernel<T, N>, sz);                                                                     \
-      za = true;                                                                                                   \
-    }                                                                                                              \
+    static const bool za = (set_smem(z_fwd_stress_kernel<T, N>, sz), true);                                       \
+    (void)za;                                                                                                      \
     z_fwd_stress_kernel<T, N><<<dim3(ntiles, nitems), z_threads<T, N>(), sz, st>>>(kq, kqc, C::NKP, dksq, nparams, \
                                                                                   part, tw);                      \
     count_launches(1);                                                                                             \

@@ -67,6 +67,8 @@ SIGNATURES = {
     "pf_domain_step": (_c_int, [_vp, _c_int]),
     "pf_domain_stress_error": (_c_int, [_vp, _dptr]),
     "pf_scft": (_c_int, [_vp, ctypes.POINTER(ScftOptions), _c_int, ctypes.POINTER(ScftResults)]),
+    "pf_scft_batch": (_c_int, [ctypes.POINTER(_vp), _c_int, ctypes.POINTER(ScftOptions), _c_int,
+                               ctypes.POINTER(ScftResults), ctypes.POINTER(_c_int), _c_int]),
     "pf_propagate": (_c_int, [_vp, _dptr, _c_double, _c_double, _c_double, _dptr, _dptr, _c_int]),
     "pf_propagate_noalloc": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _c_int, _vp]),
     "pf_set_timing": (_c_int, [_vp, _c_int]),

@@ -521,6 +521,45 @@ def scft(sys: FieldSystem, updater: AndersonUpdater, domain: Optional[DomainUpda
     return SCFTResults(r.time, r.nsteps, bool(r.converged), r.ferr, r.serr, r.fhelm, r.switch_step)
 
 
+def scft_batch(systems: Sequence[FieldSystem], updaters: Sequence[AndersonUpdater],
+               domains: Optional[Sequence[Optional[DomainUpdater]]] = None, opts: Optional[SCFTOptions] = None,
+               nthreads: int = 0, raise_on_error: bool = True):
+    """scft!(sys_i, updater_i; domain_i, opts) for many independent systems at once (a sweep).
+
+    Every system runs on its own CUDA stream; ``nthreads`` host threads (0: up to 32) drive
+    them, longest solves first, so the GPU works on up to ``nthreads`` solves concurrently.
+    Returns one SCFTResults per system, or, with ``raise_on_error=False``, (results, statuses)
+    where statuses[i] is the pf status of system i (0 = ok)."""
+    n = len(systems)
+    if len(updaters) != n:
+        raise ValueError("one AndersonUpdater per system")
+    domains = list(domains) if domains is not None else [None] * n
+    if len(domains) != n:
+        raise ValueError("one DomainUpdater (or None) per system")
+    use_domain = domains[0] is not None
+    if any((d is not None) != use_domain for d in domains):
+        raise ValueError("either every system or none has a DomainUpdater")
+    opts = opts or SCFTOptions()
+    for sys, u, d in zip(systems, updaters, domains):
+        if not isinstance(u, AndersonUpdater):
+            raise TypeError("the GPU engine implements scft! with the AndersonUpdater")
+        u._bind(sys)
+        if d is not None:
+            d._bind(sys)
+    handles = (L._vp * n)(*[s._h for s in systems])
+    o = L.ScftOptions(opts.nsteps, opts.nsout, opts.nsave, 0, opts.ftol, opts.stol, opts.mixed_switch_ferr)
+    res = (L.ScftResults * n)()
+    st = (ctypes.c_int * n)()
+    rc = L.load().pf_scft_batch(handles, n, ctypes.byref(o), 1 if use_domain else 0, res, st, int(nthreads))
+    out = [SCFTResults(r.time, r.nsteps, bool(r.converged), r.ferr, r.serr, r.fhelm, r.switch_step) for r in res]
+    if raise_on_error:
+        for i in range(n):
+            L.check(st[i], systems[i]._h)
+        L.check(rc)
+        return out
+    return out, list(st)
+
+
 # =============================================================================
 # Field initialisation and IO (src/fileio.jl)
 # =============================================================================

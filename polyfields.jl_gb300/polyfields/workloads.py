@@ -96,3 +96,37 @@ def blend3d_system(M, n=32, L=14.0, precision=None, Ns=200, seed=12345):
     gyr = np.sin(x) * np.cos(y) + np.sin(y) * np.cos(z) + np.sin(z) * np.cos(x)
     M.fieldinit(sys, seeded_fields(shape, [1, 2], seed, 0.05, gyr))
     return sys
+
+
+def hex_sweep_params(count=256, seed=12345):
+    """Parameters of a 2D hexagonal phase-diagram sweep, all drawn from one PCG64 stream:
+    grid n ~ U{32, 48, 64, 96, 128}, chiN ~ U[12, 30] (N = 100), fA ~ U[0.25, 0.50] with
+    N_A = round(100 fA) (chains built as Multiblock([A, B], [N_A, 100 - N_A]): Diblock's float
+    truncation misplaces some fA), cell a0 ~ U[4, 9], and a per-instance field seed."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sizes = np.array([32, 48, 64, 96, 128])
+    out = []
+    for i in range(count):
+        n = int(sizes[rng.integers(0, len(sizes))])
+        chin = float(rng.uniform(12.0, 30.0))
+        fa = float(rng.uniform(0.25, 0.50))
+        a0 = float(rng.uniform(4.0, 9.0))
+        out.append(dict(n=n, chi=chin / 100.0, NA=int(round(100 * fa)), a0=a0, seed=int(rng.integers(0, 2**31 - 1))))
+    return out
+
+
+def hex_instance(M, n, chi, NA, a0, seed, precision=None, Ns=100, scale=0.1, amp=1.0):
+    """One sweep instance: AB diblock (N = 100) in a 2D hexagonal cell on an n x n grid, with
+    seeded noise plus the six first-order cosines (reciprocal vectors (1,0), (0,1), (1,1) of
+    the 60-degree basis) for w_A and their negative for w_B."""
+    A, B = M.Monomer(1, 1.0), M.Monomer(2, 1.0)
+    sys = _fs(M, (n, n, 1), M.UnitCell(2, "hexagonal", a0), [A, B], precision)
+    sys.add_species(M.Multiblock([A, B], [NA, 100 - NA], [1.0, 1.0], Ns), 1.0)
+    itx = M.FloryInteraction()
+    itx.set_interaction(A, B, chi)
+    sys.add_interaction(itx)
+    shape = (1, n, n)
+    _, y, x = np.meshgrid(np.zeros(1), np.arange(n) / n, np.arange(n) / n, indexing="ij")
+    six = amp * (np.cos(2 * np.pi * x) + np.cos(2 * np.pi * y) + np.cos(2 * np.pi * (x + y)))
+    M.fieldinit(sys, seeded_fields(shape, [1, 2], seed, scale, six))
+    return sys
