@@ -42,7 +42,8 @@ enum pf_precision {
   PF_FP32 = 1   /* propagators and FFTs in float32; densities, residuals, Gram, stress sums stay float64 */
 };
 
-enum pf_grid_kind { PF_FIELD = 0, PF_DENSITY = 1, PF_RESIDUAL = 2, PF_POTENTIAL = 3 };
+/* PF_FIELD_COTANGENT: dL/dw written by pf_density_pullback (read only) */
+enum pf_grid_kind { PF_FIELD = 0, PF_DENSITY = 1, PF_RESIDUAL = 2, PF_POTENTIAL = 3, PF_FIELD_COTANGENT = 4 };
 
 typedef struct pf_system pf_system;
 
@@ -144,6 +145,20 @@ int pf_domain_stress_error(pf_system* sys, double* out);
 /* scft!(sys, AndersonUpdater; domain, opts) (src/simulate.jl:60-148) with the updaters created
  * by pf_anderson_create (required) and pf_domain_create (used when use_domain != 0). */
 int pf_scft(pf_system* sys, const pf_scft_options* opts, int use_domain, pf_scft_results* out);
+
+/* ---- pullback of density! (no counterpart in the reference: PolyFields.jl has no derivatives) ----
+ * For a scalar loss L of the pooled densities, set dL/drho_mid with pf_set_density_cotangent
+ * (NULL: zero; kept until changed), then pf_density_pullback recomputes density!(sys) at the
+ * current fields and cell and walks the adjoint of every chain backward through the same
+ * propagator kernels.  Outputs: dL/dw_mid for every monomer (pf_get_grid(...,
+ * PF_FIELD_COTANGENT, mid, out)), cell_bar[ncell] = dL/dtheta for the cell parameters
+ * (cell.jl parameter order), and nref_bar[nnref] = dL/dNref_b for the blocks of the
+ * Multiblock species in the order they were added (block lengths varied with the contour
+ * step counts fixed, ds_b = Nref_b / Ns_b: the derivative with respect to a composition f).
+ * dL/dchi is zero (chi does not enter density! at fixed fields).  Works in the handle's
+ * precision; float32 chains keep the forward solve's per-step rescaling. */
+int pf_set_density_cotangent(pf_system* sys, int mid, const double* rho_bar);
+int pf_density_pullback(pf_system* sys, double* cell_bar, int ncell, double* nref_bar, int nnref);
 
 /* Many independent scft! runs (a phase-diagram sweep: src/simulate.jl:60-148 once per
  * FieldSystem) driven together: nthreads host threads (0: min(n, 32)) take the systems in

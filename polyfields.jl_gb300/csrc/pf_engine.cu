@@ -392,6 +392,7 @@ struct System {
   std::vector<std::unique_ptr<Species>> species;
 
   DevBuf w, pot, res, rho;   // nmon * ng doubles
+  DevBuf rbar, wbar;         // adjoint: dL/drho (set by the caller) and dL/dw, nmon * ng doubles
   DevBuf part, sums, stats4, packed, cn, status;
   DevBuf twid[2];
   int tw_off[2][3] = {};  // offsets of the x, y, z tables in twid
@@ -565,7 +566,7 @@ struct System {
     mon_ids.clear();
     for (auto& kv : monomers) mon_ids.push_back(kv.first);
     // re-layout the per-monomer grids (add_monomer! zero-initialises the new monomer)
-    DevBuf* bufs[4] = {&w, &pot, &res, &rho};
+    DevBuf* bufs[6] = {&w, &pot, &res, &rho, &rbar, &wbar};
     for (DevBuf* b : bufs) {
       DevBuf nb;
       nb.alloc(sizeof(double) * ng * nmon());
@@ -1246,6 +1247,193 @@ struct System {
     }
   }
 
+  // ---------------------------------------------------------------- pullback of density!
+  // Simpson weight of offset i in a block of n intervals (multiblock.jl:209-222)
+  static double simpson_w(int i, int n) {
+    if (i == 0 || i == n) return (n == 0) ? 2.0 : 1.0;
+    return (i % 2 == 1) ? 4.0 : 2.0;
+  }
+
+  // dL/dw (into wbar), dL/dtheta of the cell and dL/dNref_b of every Multiblock block for a
+  // loss with dL/drho = rbar, at the current fields and cell.  Runs density!(sys) first so
+  // that the histories it differentiates are those of the current state.  Adjoint walks:
+  // forward chain t = Ns-1 .. 0 and backward chain s = 1 .. Ns, one contour step at a time
+  // through the forward kernels (the block operator is symmetric).
+  template <typename T>
+  void pullback_t(int p, std::vector<double>& cell_bar, std::vector<double>& nref_bar) {
+    require_ready();
+    density_t<T>(p);
+    fetch_Q();
+    const int npr = cell.np(), nw = npr + 1;
+    const CellGeom g = geom();
+    const GridDims dims{nx, ny, nz};
+    cell_bar.assign(npr, 0.0);
+    nref_bar.clear();
+    PF_CU(cudaMemsetAsync(wbar.p, 0, wbar.bytes, st));
+    int nbmax = 1;
+    for (auto& sp : species) nbmax = std::max(nbmax, sp->kind == 0 ? sp->nblocks() : 1);
+    DevBuf lamh, u, G, acc, part, wts, kq, ptrs, dpart, dots, rsp, jobsd;
+    lamh.alloc(sizeof(T) * 2 * ng);
+    u.alloc(sizeof(T) * 2 * ng);
+    G.alloc(sizeof(double) * nbmax * ng);
+    acc.alloc(sizeof(double) * nbmax * nw);
+    const int M = zM(p);
+    const long ntiles = ((nx / 2 + 1) * (long)ny + M - 1) / M;
+    part.alloc(sizeof(double) * (size_t)std::max<long>(1, ntiles) * nw);
+    wts.alloc(sizeof(double) * (size_t)nbmax * nw * nk);
+    kq.alloc(sizeof(Cx<T>) * 2 * nk);
+    dpart.alloc(sizeof(double) * kRedBlocks);
+    dots.alloc(sizeof(double) * 4 * kMaxMon);
+    rsp.alloc(sizeof(double) * nmon() * ng);
+    T* lam = lamh.as<T>();
+    T* rr = lam + ng;
+    T* u1 = u.as<T>();
+    T* u2 = u1 + ng;
+    Cx<T>* k1 = kq.as<Cx<T>>();
+    Cx<T>* k2 = k1 + nk;
+    {
+      const void* hp[4] = {u1, u2, k1, k2};
+      ptrs.alloc(sizeof(hp));
+      PF_CU(cudaMemcpyAsync(ptrs.p, hp, sizeof(hp), cudaMemcpyHostToDevice, st));
+    }
+    const T* const* src_dev = reinterpret_cast<const T* const*>(ptrs.as<void*>());
+    Cx<T>* const* dst_dev = reinterpret_cast<Cx<T>* const*>(ptrs.as<void*>() + 2);
+    const double* rb = rbar.as<double>();
+    auto dot_host = [&](const double* a, const double* b) {
+      launch_ddot(a, b, ng, dpart.as<double>(), dots.as<double>(), st);
+      double v = 0.0;
+      PF_CU(cudaMemcpyAsync(&v, dots.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+      PF_CU(cudaStreamSynchronize(st));
+      return v;
+    };
+    for (auto& spp : species) {
+      Species& sp = *spp;
+      if (sp.kind == 1) {  // point species (point.jl:36-58)
+        const int mid = sp.mids[0];
+        const double vol = monomers.at(mid).first;
+        PF_CU(cudaMemsetAsync(rsp.p, 0, rsp.bytes, st));
+        launch_point_density(grid_ptr(rsp, mid), grid_ptr(w, mid), vol, sp.phi, sp.Qdev.as<double>(), ng, st);
+        const double S = dot_host(rb + (long)mon_index(mid) * ng, grid_ptr(rsp, mid));
+        launch_adj_point(grid_ptr(wbar, mid), grid_ptr(rsp, mid), rb + (long)mon_index(mid) * ng, grid_ptr(w, mid),
+                         vol, S, (double)ng * sp.Q, ng, st);
+        continue;
+      }
+      const int nb = sp.nblocks(), Ns = sp.Ns;
+      const bool homo = nb == 1;
+      const T* q = sp.q[p].as<T>();
+      const T* qc = homo ? nullptr : sp.qc[p].as<T>();
+      auto b0 = [&](int b) { return sp.begin_block[b] - 1; };
+      auto b1 = [&](int b) { return sp.begin_block[b + 1] - 1; };
+      // Simpson contribution of each block: <rbar_m, phi rho_block>
+      std::vector<double> contrib(nb);
+      double S = 0.0;
+      for (int b = 0; b < nb; ++b) {
+        PF_CU(cudaMemsetAsync(rsp.p, 0, rsp.bytes, st));
+        SimpsonBlocks sb{};
+        sb.nblocks = 1;
+        sb.mon[0] = mon_index(sp.mid_block[b]);
+        sb.bgn[0] = b0(b);
+        sb.end[0] = b1(b);
+        sb.ds[0] = sp.ds_block[b];
+        launch_simpson<T>(rsp.as<double>(), q, homo ? nullptr : qc, homo, Ns, ng, sb, sp.phi, sp.Nref,
+                          sp.Qdev.as<double>(), scaled(p) ? sp.fac.as<double>() : nullptr, st);
+        contrib[b] = dot_host(rb + (long)sb.mon[0] * ng, rsp.as<double>() + (long)sb.mon[0] * ng);
+        S += contrib[b];
+      }
+      double meanq = sp.Q;
+      if (scaled(p)) {
+        PF_CU(cudaMemcpyAsync(&meanq, sp.meanq.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+        PF_CU(cudaStreamSynchronize(st));
+      }
+      const double dq = -S / (meanq * (double)ng);  // through Q = mean(q_Ns), rescaled
+      for (int b = 0; b < nb; ++b)
+        launch_adj_weights(wts.as<double>() + (size_t)b * nw * nk, g, npr, sp.ds_block[b], sp.b_block[b],
+                           1.0 / (double)ng, nk, st);
+      PF_CU(cudaMemsetAsync(G.p, 0, G.bytes, st));
+      PF_CU(cudaMemsetAsync(acc.p, 0, acc.bytes, st));
+      // one-step jobs: forward step t at ops[t], backward step t' = Ns - s at ops[Ns + t']
+      const StepOp<T>* ops = sp.ops[p].as<StepOp<T>>();
+      std::vector<ChainJob<T>> hj(2 * (size_t)Ns);
+      for (int t = 0; t < 2 * Ns; ++t)
+        hj[t] = ChainJob<T>{lam, ops + t, nz > 1 ? k1 : nullptr, nullptr, nullptr, 0, +1, 1, 0};
+      jobsd.alloc(sizeof(ChainJob<T>) * hj.size());
+      PF_CU(cudaMemcpyAsync(jobsd.p, hj.data(), jobsd.bytes, cudaMemcpyHostToDevice, st));
+      const ChainJob<T>* jd = jobsd.as<ChainJob<T>>();
+      // adjoint sources at contour point s: chain q (qs = qc_s) or chain qc (qs = q_s)
+      auto src_at = [&](int s, bool chain_q) {
+        AdjSrc<T> a;
+        for (int b = 0; b < nb && a.n < 3; ++b) {
+          if (s < b0(b) || s > b1(b)) continue;
+          const int n = b1(b) - b0(b);
+          double wsum = simpson_w(s - b0(b), n);
+          if (homo) wsum += simpson_w(Ns - s - b0(b), n);  // qc_s = q_{Ns-s}
+          a.coef[a.n] = sp.phi * sp.ds_block[b] / 3.0 * wsum / sp.Nref;
+          a.rb[a.n] = rb + (long)mon_index(sp.mid_block[b]) * ng;
+          a.qs[a.n] = chain_q ? (homo ? q + (long)(Ns - s) * ng : qc + (long)s * ng) : q + (long)s * ng;
+          ++a.n;
+        }
+        a.fac = scaled(p) ? sp.fac.as<double>() + s : nullptr;
+        a.Qdev = sp.Qdev.as<double>();
+        return a;
+      };
+      // one adjoint step: ybar in lam, x -> y the primal step, block b, factor cfac
+      auto step = [&](int job, int b, const T* x, const T* y, const float* cfac, const AdjSrc<T>& src) {
+        const T* lwb = sp.lw[p][b]->as<T>();
+        const T* ldb = sp.ld[p][b]->as<T>();
+        launch_adj_lw_pair<T>(u1, u2, lwb, x, lam, ng, st);
+        const int nparts = launch_grad_transform<T>(u1, u2, k1, k2, src_dev, dst_dev, dims,
+                                                    wts.as<double>() + (size_t)b * nw * nk, nw, part.as<double>(),
+                                                    tw<T>(p), st);
+        launch_adj_accum(acc.as<double>() + (size_t)b * nw, part.as<double>(), nparts, nw, cfac, st);
+        ChainHost<T> h;
+        h.kbuf = nz > 1 ? k1 : nullptr;
+        h.nsteps = 1;
+        h.ld = &ldb;
+        launch_chains<T>(jd + job, 1, 1, dims, tw<T>(p), st, &h);
+        launch_adj_finish<T>(lam, rr, lam, x, y, G.as<double>() + (size_t)b * ng, cfac, src, ng, st);
+        check_launch();
+      };
+      // forward chain q_{t+1} = A q_t: adjoint from t = Ns down to 0
+      launch_adj_init<T>(lam, src_at(Ns, true), dq, ng, st);
+      for (int t = Ns - 1; t >= 0; --t) {
+        int b = 0;
+        while (!(b0(b) <= t && t < b1(b))) ++b;
+        const float* cf = scaled(p) ? sp.csc[0].as<float>() + t : nullptr;
+        step(t, b, q + (long)t * ng, q + (long)(t + 1) * ng, cf, src_at(t, true));
+      }
+      if (!homo) {
+        // backward chain qc_{s-1} = A qc_s: adjoint from s = 0 up to Ns
+        launch_adj_init<T>(lam, src_at(0, false), 0.0, ng, st);
+        for (int s = 1; s <= Ns; ++s) {
+          int b = 0;
+          while (!(b0(b) < s && s <= b1(b))) ++b;
+          const int tp = Ns - s;
+          const float* cf = scaled(p) ? sp.csc[1].as<float>() + tp : nullptr;
+          step(Ns + tp, b, qc + (long)s * ng, qc + (long)(s - 1) * ng, cf, src_at(s, false));
+        }
+      }
+      // w gradients and the ds / Nref terms of every block
+      std::vector<double> hacc((size_t)nb * nw);
+      PF_CU(cudaMemcpyAsync(hacc.data(), acc.p, sizeof(double) * hacc.size(), cudaMemcpyDeviceToHost, st));
+      for (int b = 0; b < nb; ++b) {
+        const int mid = sp.mid_block[b];
+        const double vol = monomers.at(mid).first;
+        const double* Gb = G.as<double>() + (size_t)b * ng;
+        launch_daxpy(grid_ptr(wbar, mid), Gb, -sp.ds_block[b] * vol / 2.0, ng, st);
+        const double wg = dot_host(grid_ptr(w, mid), Gb);
+        for (int j = 0; j < npr; ++j) cell_bar[j] += hacc[(size_t)b * nw + j];
+        const double dds = hacc[(size_t)b * nw + npr] - vol / 2.0 * wg + contrib[b] / sp.ds_block[b];
+        nref_bar.push_back(dds / (double)(b1(b) - b0(b)) - S / sp.Nref);
+      }
+    }
+    PF_CU(cudaStreamSynchronize(st));
+    check_pipe(p);
+  }
+  void pullback(std::vector<double>& cell_bar, std::vector<double>& nref_bar) {
+    if (prec == 0) pullback_t<double>(0, cell_bar, nref_bar);
+    else pullback_t<float>(1, cell_bar, nref_bar);
+  }
+
   // ---------------------------------------------------------------- scft! (simulate.jl:60-148)
   static bool isconverged(double ferr, double ftol, double serr, double stol, bool vcell) {
     bool fc = false, sc = true;
@@ -1526,7 +1714,12 @@ int pf_set_field(pf_system* sys, int mid, const double* w) {
 int pf_get_grid(pf_system* sys, int kind, int mid, double* out) {
   return guard(sys, [&](pf::System& s) {
     if (!out) throw pf::PFError(PF_EARG, "null output");
-    pf::DevBuf* b = kind == PF_FIELD ? &s.w : kind == PF_DENSITY ? &s.rho : kind == PF_RESIDUAL ? &s.res : &s.pot;
+    if (kind < PF_FIELD || kind > PF_FIELD_COTANGENT) throw pf::PFError(PF_EARG, "unknown grid kind");
+    pf::DevBuf* b = kind == PF_FIELD      ? &s.w
+                    : kind == PF_DENSITY  ? &s.rho
+                    : kind == PF_RESIDUAL ? &s.res
+                    : kind == PF_POTENTIAL ? &s.pot
+                                           : &s.wbar;
     PF_CU(cudaMemcpyAsync(out, s.grid_ptr(*b, mid), sizeof(double) * s.ng, cudaMemcpyDeviceToHost, s.st));
     PF_CU(cudaStreamSynchronize(s.st));
   });
@@ -1653,6 +1846,26 @@ int pf_scft(pf_system* sys, const pf_scft_options* opts, int use_domain, pf_scft
   return guard(sys, [&](pf::System& s) {
     if (!opts || !out) throw pf::PFError(PF_EARG, "null options/results");
     *out = s.scft(*opts, use_domain != 0);
+  });
+}
+
+int pf_set_density_cotangent(pf_system* sys, int mid, const double* rho_bar) {
+  return guard(sys, [&](pf::System& s) {
+    double* dst = s.grid_ptr(s.rbar, mid);
+    if (rho_bar) PF_CU(cudaMemcpyAsync(dst, rho_bar, sizeof(double) * s.ng, cudaMemcpyHostToDevice, s.st));
+    else PF_CU(cudaMemsetAsync(dst, 0, sizeof(double) * s.ng, s.st));
+    PF_CU(cudaStreamSynchronize(s.st));
+  });
+}
+
+int pf_density_pullback(pf_system* sys, double* cell_bar, int ncell, double* nref_bar, int nnref) {
+  return guard(sys, [&](pf::System& s) {
+    std::vector<double> cb, nb;
+    s.pullback(cb, nb);
+    if (cell_bar)
+      for (int i = 0; i < std::min(ncell, (int)cb.size()); ++i) cell_bar[i] = cb[i];
+    if (nref_bar)
+      for (int i = 0; i < std::min(nnref, (int)nb.size()); ++i) nref_bar[i] = nb[i];
   });
 }
 

@@ -109,6 +109,49 @@ struct ChainHost {
 template <typename T>
 void launch_chains(const ChainJob<T>* jobs_dev, int njobs, int maxsteps, const GridDims& d, const Twiddles<T>& tw,
                    cudaStream_t st, const ChainHost<T>* hosts, const Branches* br = nullptr);
+// Adjoint of the bond operator: rfft of the real grids u1, u2 and, for j < nw, the sums
+// sum_k mult_k Re(U1_k conj U2_k) wts[j * Nk + k] (mult_k: Hermitian multiplicity) into
+// part[i * nw + j] for i < the returned number of partial blocks.  3D grids use the
+// half-spectrum scratch k1, k2 and the device pointer arrays src_dev = {u1, u2},
+// dst_dev = {k1, k2}; Nz == 1 uses k1 only.  nw <= kMaxParams + 1.
+template <typename T>
+int launch_grad_transform(const T* u1, const T* u2, Cx<T>* k1, Cx<T>* k2, const T* const* src_dev,
+                          Cx<T>* const* dst_dev, const GridDims& d, const double* wts, int nw, double* part,
+                          const Twiddles<T>& tw, cudaStream_t st);
+// Gradient weights of a block's bond operator (pf_mde_fp64.cu): nparams + 1 rows of Nk.
+void launch_adj_weights(double* wts, const CellGeom& g, int nparams, double ds, double b, double scale, long nk,
+                        cudaStream_t st);
+// ---- adjoint elementwise pieces (pf_adjoint.cu)
+// Source terms of the adjoint at one contour point: sum_i coef[i] * rb[i] * qs[i], times
+// f = fac ? *fac : 1 / *Qdev.
+template <typename T>
+struct AdjSrc {
+  int n = 0;
+  const double* rb[3] = {};
+  const T* qs[3] = {};
+  double coef[3] = {};
+  const double* fac = nullptr;
+  const double* Qdev = nullptr;
+};
+// u1 = lw * x, u2 = lw * ybar
+template <typename T>
+void launch_adj_lw_pair(T* u1, T* u2, const T* lw, const T* x, const T* ybar, long n, cudaStream_t st);
+// G += ybar * y + c * x * r; lam = c * r + sources (c = cfac ? *cfac : 1); lam may alias ybar
+template <typename T>
+void launch_adj_finish(T* lam, const T* r, const T* ybar, const T* x, const T* y, double* G, const float* cfac,
+                       const AdjSrc<T>& src, long n, cudaStream_t st);
+// lam = sources + dq (dq added to every point)
+template <typename T>
+void launch_adj_init(T* lam, const AdjSrc<T>& src, double dq, long n, cudaStream_t st);
+// acc[j] += c * sum_i part[i * nw + j]  (c = cfac ? *cfac : 1; one block, fixed order)
+void launch_adj_accum(double* acc, const double* part, int nparts, int nw, const float* cfac, cudaStream_t st);
+// Point species: wbar += -vol * rho * rb + S * vol * exp(-vol * w) / (Ng * Q)
+void launch_adj_point(double* wbar, const double* rho, const double* rb, const double* w, double vol, double S,
+                      double ngQ, long n, cudaStream_t st);
+// y += a * x (float64 grids)
+void launch_daxpy(double* y, const double* x, double a, long n, cudaStream_t st);
+// sum_x a_x * b_x into *out (device), float64, deterministic
+void launch_ddot(const double* a, const double* b, long n, double* part, double* out, cudaStream_t st);
 // Nonzero when a pipelined kernel of this precision gave up waiting on a copy since the
 // last call (reads and clears a device flag; synchronises the stream).
 template <typename T>

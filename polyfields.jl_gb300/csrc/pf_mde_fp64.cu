@@ -13,6 +13,38 @@ void launch_dksq(double* dk, const CellGeom& g, int nparams, long nk, cudaStream
   count_launches(1);
 }
 
+// Weights of the bond-operator gradient of one block (rows j < nparams: cell parameter j,
+// row nparams: the block's ds) on the half spectrum:
+//   LD_k = exp(-ds b^2 ksq_k / 6) * scale,  wts[j][k] = LD_k * (-ds b^2 / 6) * dksq_j,k,
+//   wts[nparams][k] = LD_k * (-b^2 / 6) * ksq_k.
+static __global__ void adj_weights_kernel(double* __restrict__ wts, CellGeom g, int nparams, double ds, double b,
+                                          double scale) {
+  const long nk = (long)(g.nx / 2 + 1) * g.ny * g.nz;
+  const double b2 = b * b;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nk; i += (long)gridDim.x * blockDim.x) {
+    int ix, iy, iz;
+    spectral_index(g, i, ix, iy, iz);
+    const double ksq = ksq_at(g, ix, iy, iz);
+    const double ld = exp(-ds * b2 * ksq / 6.0) * scale;
+    const double j[3] = {(double)ix, fold_index(iy, g.ny), fold_index(iz, g.nz)};
+    for (int p = 0; p < nparams; ++p) {
+      double acc = 0.0;
+      for (int l = 0; l < g.dim; ++l)
+        for (int m = 0; m < g.dim; ++m) acc += j[l] * j[m] * g.dGG[(l * 3 + m) * kMaxParams + p];
+      wts[p * nk + i] = ld * (-ds * b2 / 6.0) * acc;
+    }
+    wts[nparams * nk + i] = ld * (-b2 / 6.0) * ksq;
+  }
+}
+
+void launch_adj_weights(double* wts, const CellGeom& g, int nparams, double ds, double b, double scale, long nk,
+                        cudaStream_t st) {
+  int blocks = (int)((nk + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  adj_weights_kernel<<<blocks, 256, 0, st>>>(wts, g, nparams, ds, b, scale);
+  count_launches(1);
+}
+
 namespace {
 template <int N>
 int twiddle_table_n(double* re, double* im, int max_entries) {

@@ -977,6 +977,124 @@ __global__ void __launch_bounds__(512)
   }
 }
 
+// ------------------------------------------------------------------ adjoint transforms
+// Gradient sums of the bond operator: for real grids u1, u2 with half spectra U1 = rfft(u1),
+// U2 = rfft(u2), part[.. * nw + j] = sum_k mult_k Re(U1_k conj U2_k) wts[j * Nk + k], where
+// mult_k is the Hermitian multiplicity of the half spectrum (1 on the kx = 0 and kx = Nx/2
+// planes, 2 elsewhere).  Nz == 1: one CTA transforms u1 (its spectrum parked in k1, same
+// thread -> element mapping in both passes) and then u2.
+template <typename T, int NX, int NY>
+__global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
+    grad_plane_kernel(const T* __restrict__ u1, const T* __restrict__ u2, Cx<T>* __restrict__ k1,
+                      const double* __restrict__ wts, int nw, double* __restrict__ part, Twiddles<T> twg) {
+  using C = PlaneCfg<NX, NY>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Cx<T>* S = reinterpret_cast<Cx<T>*>(smem_raw);
+  __shared__ Cx<T> twx[C::TWX], twy[C::TWY];
+  __shared__ double red[kMaxParams + 1][32];
+  stage<T>(twx, twg.x, C::TWX);
+  if (NY > 1) stage<T>(twy, twg.y, C::TWY);
+  const int p = group_index<C::GX, C::SP>(threadIdx.x / C::GX), gx = threadIdx.x % C::GX;
+  const bool xact = p < C::NPAIR;
+  const int c = group_index<C::GY, C::SC>(threadIdx.x / C::GY), gy = threadIdx.x % C::GY;
+  const bool yact = NY > 1 && c < C::KX;
+  double acc[kMaxParams + 1];
+  for (int j = 0; j <= kMaxParams; ++j) acc[j] = 0.0;
+  auto visit = [&](int pass, int kk, int kx, const Cx<T>& v) {
+    if (pass == 0) {
+      k1[kk] = v;
+    } else {
+      const Cx<T> a = k1[kk];
+      const double m = (kx == 0 || 2 * kx == NX) ? 1.0 : 2.0;
+      const double prod = m * ((double)a.x * (double)v.x + (double)a.y * (double)v.y);
+      for (int j = 0; j < nw; ++j) acc[j] += prod * wts[(long)j * C::NKP + kk];
+    }
+  };
+  __syncthreads();
+  for (int pass = 0; pass < 2; ++pass) {
+    XRegs<T, NX> r;
+    if (xact) load_regs<T, NX, NY>(r, p, gx, nullptr, pass == 0 ? u1 : u2);
+    if constexpr (NY == 1) {
+      BARegs<T, NX> w;
+      row_forward_1d<T, NX>(S, twx, r, w, gx, xact);
+      if (xact) {
+#pragma unroll
+        for (int b = 0; b < JoinBA<NX>::BPT; ++b)
+#pragma unroll
+          for (int tt = 0; tt < JoinBA<NX>::R; ++tt) {
+            const int x = JoinBA<NX>::pos(gx, b, tt);
+            if (x <= NX / 2) visit(pass, x, x, w.v[b][tt]);
+          }
+      }
+      __syncwarp();
+    } else {
+      x_forward_from_regs<T, NX, NY>(S, twx, r, p, gx, xact);
+      __syncthreads();
+      BARegs<T, NY> w;
+      y_forward_to_regs<T, NX, NY>(S, twy, w, c, gy, yact);
+      if (yact) {
+#pragma unroll
+        for (int b = 0; b < JoinBA<NY>::BPT; ++b)
+#pragma unroll
+          for (int tt = 0; tt < JoinBA<NY>::R; ++tt) {
+            const int ky = JoinBA<NY>::pos(gy, b, tt);
+            visit(pass, c * NY + ky, c, w.v[b][tt]);
+          }
+      }
+    }
+    __syncthreads();
+  }
+  for (int j = 0; j < nw; ++j) {
+    const double v = block_sum(acc[j], red[j]);
+    if (threadIdx.x == 0) part[j] = v;
+  }
+}
+
+// 3D, pencil pass: z transforms of the two plane-transformed spectra k1, k2 ([kz][kx][ky])
+// and the weighted sums over the tile.  Output part[tile * nw + j].
+template <typename T, int NZ>
+__global__ void __launch_bounds__(512)
+    z_fwd_grad_kernel(const Cx<T>* __restrict__ k1, const Cx<T>* __restrict__ k2, int nkp, int nx, int ny,
+                      const double* __restrict__ wts, int nw, double* __restrict__ part, Twiddles<T> twg) {
+  constexpr int M = ZCfg<T>::M;
+  constexpr int LDT = NZ + pencil_pad<NZ>();
+  constexpr int G = Plan<NZ>::G;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Cx<T>* A = reinterpret_cast<Cx<T>*>(smem_raw);
+  Cx<T>* B = A + M * LDT;
+  __shared__ Cx<T> twz[tw_total<NZ>()];
+  __shared__ double red[kMaxParams + 1][32];
+  stage<T>(twz, twg.z, tw_total<NZ>());
+  __syncthreads();
+  const long nk = (long)nkp * NZ;
+  const int m0 = blockIdx.x * M;
+  const int mm = threadIdx.x / G, g = threadIdx.x % G;
+  const bool active = mm < M && m0 + mm < nkp;
+  const long col = m0 + (active ? mm : 0);
+  BARegs<T, NZ> wa, wb;
+  z_forward_to_regs<T, NZ>(k1, nkp, col, A + (active ? mm : 0) * LDT, twz, wa, g, active);
+  z_forward_to_regs<T, NZ>(k2, nkp, col, B + (active ? mm : 0) * LDT, twz, wb, g, active);
+  double acc[kMaxParams + 1];
+  for (int j = 0; j <= kMaxParams; ++j) acc[j] = 0.0;
+  if (active) {
+    const int kx = (int)(col / ny);
+    const double m = (kx == 0 || 2 * kx == nx) ? 1.0 : 2.0;
+#pragma unroll
+    for (int b = 0; b < JoinBA<NZ>::BPT; ++b)
+#pragma unroll
+      for (int tt = 0; tt < JoinBA<NZ>::R; ++tt) {
+        const long kk = (long)JoinBA<NZ>::pos(g, b, tt) * nkp + col;
+        const double prod =
+            m * ((double)wa.v[b][tt].x * (double)wb.v[b][tt].x + (double)wa.v[b][tt].y * (double)wb.v[b][tt].y);
+        for (int j = 0; j < nw; ++j) acc[j] += prod * wts[j * nk + kk];
+      }
+  }
+  for (int j = 0; j < nw; ++j) {
+    const double v = block_sum(acc[j], red[j]);
+    if (threadIdx.x == 0) part[(long)blockIdx.x * nw + j] = v;
+  }
+}
+
 // ------------------------------------------------------------------ host launchers
 template <typename K>
 static void set_smem(K kernel, size_t bytes) {
@@ -1180,6 +1298,62 @@ static void stress_shape(const StressItem<T>* items, int nitems, const T* const*
   }
 }
 
+template <typename T, int NX, int NY>
+static int grad_shape(const T* u1, const T* u2, Cx<T>* k1, Cx<T>* k2, const T* const* src, Cx<T>* const* dst, int nz,
+                      const double* wts, int nw, double* part, const Twiddles<T>& tw, cudaStream_t st) {
+  using C = PlaneCfg<NX, NY>;
+  constexpr size_t sp = plane_smem<T, NX, NY>();
+  static const bool attr = [] {
+    set_smem(grad_plane_kernel<T, NX, NY>, sp);
+    if constexpr (NY > 1) set_smem(xy_fwd_kernel<T, NX, NY>, sp);
+    return true;
+  }();
+  (void)attr;
+  if (nz == 1) {
+    grad_plane_kernel<T, NX, NY><<<1, C::THREADS, sp, st>>>(u1, u2, k1, wts, nw, part, tw);
+    count_launches(1);
+    return 1;
+  }
+  if constexpr (NY > 1) {
+    xy_fwd_kernel<T, NX, NY><<<dim3(nz, 2), C::THREADS, sp, st>>>(src, dst, tw);
+    count_launches(1);
+    constexpr int M = ZCfg<T>::M;
+    const int ntiles = (C::NKP + M - 1) / M;
+    switch (nz) {
+#define PF_Z(N)                                                                                         \
+  case N: {                                                                                             \
+    const size_t sz = 2 * sizeof(Cx<T>) * (size_t)(N + pencil_pad<N>()) * M;                            \
+    static const bool za = (set_smem(z_fwd_grad_kernel<T, N>, sz), true);                               \
+    (void)za;                                                                                           \
+    z_fwd_grad_kernel<T, N><<<ntiles, z_threads<T, N>(), sz, st>>>(k1, k2, C::NKP, NX, NY, wts, nw, part, \
+                                                                  tw);                                 \
+    count_launches(1);                                                                                  \
+  } break;
+      PF_Z_LENGTHS(PF_Z)
+#undef PF_Z
+      default:
+        break;
+    }
+    return ntiles;
+  }
+  return 0;
+}
+
+template <typename T>
+int launch_grad_transform(const T* u1, const T* u2, Cx<T>* k1, Cx<T>* k2, const T* const* src_dev,
+                          Cx<T>* const* dst_dev, const GridDims& d, const double* wts, int nw, double* part,
+                          const Twiddles<T>& tw, cudaStream_t st) {
+  switch (shape_key(d.nx, d.ny)) {
+#define PF_S(A, B)                                                                                  \
+  case A * 1024 + B:                                                                                \
+    return grad_shape<T, A, B>(u1, u2, k1, k2, src_dev, dst_dev, d.nz, wts, nw, part, tw, st);
+    PF_PLANE_SHAPES(PF_S)
+#undef PF_S
+    default:
+      return 0;
+  }
+}
+
 // Whether kernels exist for this grid (and fit the shared memory of one CTA).
 template <typename T>
 bool shape_supported(int nx, int ny, int nz) {
@@ -1260,6 +1434,9 @@ void launch_stress(const StressItem<T>* items, int nitems, const T* const* src_q
   template void launch_chains<T>(const ChainJob<T>*, int, int, const GridDims&, const Twiddles<T>&,       \
                                  cudaStream_t, const ChainHost<T>*, const Branches*);                     \
   template int take_pipe_status<T>(cudaStream_t);                                                          \
+  template int launch_grad_transform<T>(const T*, const T*, Cx<T>*, Cx<T>*, const T* const*, Cx<T>* const*,   \
+                                        const GridDims&, const double*, int, double*, const Twiddles<T>&,     \
+                                        cudaStream_t);                                                          \
   template void launch_stress<T>(const StressItem<T>*, int, const T* const*, const T* const*, Cx<T>* const*, \
                                  Cx<T>* const*, const GridDims&, const double*, int, double*,              \
                                  const Twiddles<T>&, cudaStream_t);

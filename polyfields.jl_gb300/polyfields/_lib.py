@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(_HERE, "libpolyfields_gpu.so")
 (PF_OK, PF_EARG, PF_ECUDA, PF_ENAN, PF_ESINGULAR, PF_ETIMEOUT, PF_ESTATE, PF_ENOMEM, PF_EUNSUPPORTED,
  PF_ETOOLARGE) = range(10)
 PF_FP64, PF_FP32 = 0, 1
-PF_FIELD, PF_DENSITY, PF_RESIDUAL, PF_POTENTIAL = range(4)
+PF_FIELD, PF_DENSITY, PF_RESIDUAL, PF_POTENTIAL, PF_FIELD_COTANGENT = range(5)
 
 # Every symbol the header declares, with (restype, argtypes).
 _c_int, _c_double, _c_char_p, _vp = ctypes.c_int, ctypes.c_double, ctypes.c_char_p, ctypes.c_void_p
@@ -67,6 +67,8 @@ SIGNATURES = {
     "pf_domain_step": (_c_int, [_vp, _c_int]),
     "pf_domain_stress_error": (_c_int, [_vp, _dptr]),
     "pf_scft": (_c_int, [_vp, ctypes.POINTER(ScftOptions), _c_int, ctypes.POINTER(ScftResults)]),
+    "pf_set_density_cotangent": (_c_int, [_vp, _c_int, _dptr]),
+    "pf_density_pullback": (_c_int, [_vp, _dptr, _c_int, _dptr, _c_int]),
     "pf_scft_batch": (_c_int, [ctypes.POINTER(_vp), _c_int, ctypes.POINTER(ScftOptions), _c_int,
                                ctypes.POINTER(ScftResults), ctypes.POINTER(_c_int), _c_int]),
     "pf_propagate": (_c_int, [_vp, _dptr, _c_double, _c_double, _c_double, _dptr, _dptr, _c_int]),

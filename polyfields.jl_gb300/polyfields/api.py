@@ -359,6 +359,40 @@ class FieldSystem:
         L.check(L.load().pf_get_propagator(self._h, isp, 1 if conjugate else 0, s, L.dptr(out)), self._h)
         return out
 
+    def density_pullback(self, rho_bar: Dict[int, np.ndarray]) -> Dict:
+        """Pullback of density!(sys) for a loss L with dL/drho_m = rho_bar[m] (monomers not
+        listed: zero).  Recomputes the density at the current fields and cell, then returns
+        {"w": {mid: dL/dw_mid}, "cell": dL/dtheta, "Nref_block": [per species, dL/dNref_b of
+        each block (empty for point species)], "chi": {pair: 0.0}}."""
+        lib = L.load()
+        for mid in self.monomers:
+            arr = rho_bar.get(mid)
+            if arr is None:
+                L.check(lib.pf_set_density_cotangent(self._h, mid, None), self._h)
+            else:
+                a = np.ascontiguousarray(arr, dtype=np.float64)
+                if a.shape != self.shape:
+                    raise ValueError(f"cotangent of monomer {mid} has shape {a.shape}, expected {self.shape}")
+                L.check(lib.pf_set_density_cotangent(self._h, mid, L.dptr(a)), self._h)
+        npr = len(self.cell.params)
+        nblk = [len(sp.N_block) if isinstance(sp, Multiblock) else 0 for sp in self.species]
+        cell_bar = np.zeros(max(1, npr))
+        nref = np.zeros(max(1, sum(nblk)))
+        L.check(lib.pf_density_pullback(self._h, L.dptr(cell_bar), npr, L.dptr(nref), sum(nblk)), self._h)
+        out = {"w": {}, "cell": cell_bar[:npr].copy(), "Nref_block": [], "chi": {}}
+        for mid in self.monomers:
+            g = np.empty(self.shape)
+            L.check(lib.pf_get_grid(self._h, L.PF_FIELD_COTANGENT, mid, L.dptr(g)), self._h)
+            out["w"][mid] = g
+        k = 0
+        for n in nblk:
+            out["Nref_block"].append(list(nref[k:k + n]))
+            k += n
+        for itx in self.interactions:
+            for pair in itx.chis:
+                out["chi"][pair] = 0.0
+        return out
+
     def set_timing(self, enable: bool) -> None:
         L.check(L.load().pf_set_timing(self._h, 1 if enable else 0), self._h)
 
