@@ -1,6 +1,7 @@
 """Time-to-solution of the large-blend system: plain FP64 solve vs FP32 iterations with FP64 polish.
 
-    python polyfields.jl_gb300/converge.py [--n 128] [--nsteps 4000] [--switch 1e-5] [--modes fp64,mixed]
+    python polyfields.jl_gb300/converge.py [--n 128] [--nsteps 4000] [--switch 1e-5] [--modes mixed,fp64]
+        [--nhist 20] [--iter-euler 1] [--lam-euler 0.01] [--nskip 5] [--nper 20] [--fixed-cell]
 
 Builds the large blend (AB diblock N100 fA0.4 at phi 0.8 + A homopolymer N50 at phi 0.2,
 chi 0.2, Ns 200, cubic cell L0 = 14, double-gyroid start plus 0.05 seeded noise) on an n^3
@@ -21,13 +22,15 @@ import polyfields as pf  # noqa: E402
 from polyfields import workloads as W  # noqa: E402
 
 
-def run(n, precision, nsteps, switch, ftol, stol, nsout):
+def run(n, precision, nsteps, switch, ftol, stol, nsout, a):
     sysm = W.blend3d_system(pf, n=n, precision=precision)
     sysm.synchronize()
     opts = pf.SCFTOptions(nsteps=nsteps, ftol=ftol, stol=stol, nsout=nsout,
                           mixed_switch_ferr=switch if precision == "fp32" else 0.0)
+    upd = pf.AndersonUpdater(nhist=a.nhist, iter_euler=a.iter_euler, lam_euler=a.lam_euler)
+    dom = None if a.fixed_cell else pf.DomainUpdater(nskip=a.nskip, nper=a.nper)
     t0 = time.perf_counter()
-    r = pf.scft(sysm, pf.AndersonUpdater(nhist=20), domain=pf.DomainUpdater(nskip=5, nper=20), opts=opts)
+    r = pf.scft(sysm, upd, domain=dom, opts=opts)
     sysm.synchronize()
     wall = time.perf_counter() - t0
     return {"precision": "mixed" if precision == "fp32" else "fp64", "wall_s": wall, "iterations": r.nsteps,
@@ -44,12 +47,20 @@ def main():
     ap.add_argument("--stol", type=float, default=1e-8)
     ap.add_argument("--modes", default="mixed,fp64")
     ap.add_argument("--nsout", type=int, default=0)
+    ap.add_argument("--nhist", type=int, default=20)
+    ap.add_argument("--iter-euler", type=int, default=1)
+    ap.add_argument("--lam-euler", type=float, default=0.01)
+    ap.add_argument("--nskip", type=int, default=5)
+    ap.add_argument("--nper", type=int, default=20)
+    ap.add_argument("--fixed-cell", action="store_true", help="no DomainUpdater (cell held at L0)")
     a = ap.parse_args()
-    out = {"workload": f"large blend {a.n}^3, Ns 200, nhist 20, nskip 5, nper 20", "ftol": a.ftol, "stol": a.stol,
+    cellmode = "fixed cell L0 = 14" if a.fixed_cell else f"DomainUpdater nskip {a.nskip} nper {a.nper}"
+    out = {"workload": f"large blend {a.n}^3, Ns 200, Anderson nhist {a.nhist} (iter_euler {a.iter_euler}, "
+                       f"lam_euler {a.lam_euler}), {cellmode}", "ftol": a.ftol, "stol": a.stol,
            "switch_ferr": a.switch, "runs": []}
     for mode in a.modes.split(","):
         prec = "fp32" if mode == "mixed" else "fp64"
-        out["runs"].append(run(a.n, prec, a.nsteps, a.switch, a.ftol, a.stol, a.nsout))
+        out["runs"].append(run(a.n, prec, a.nsteps, a.switch, a.ftol, a.stol, a.nsout, a))
         print(json.dumps(out["runs"][-1]), file=sys.stderr, flush=True)
     runs = {r["precision"]: r for r in out["runs"]}
     if "mixed" in runs and "fp64" in runs:

@@ -1134,6 +1134,20 @@ struct System {
     and_.is_setup = true;
   }
 
+  // Mixed precision: at the float32 -> float64 switch the history holds residuals with
+  // float32 rounding (~1e-7 relative), as large as the differences the float64 phase has to
+  // resolve; the history restarts from the current field exactly as setup! starts it
+  // (anderson.jl:54-92: iteration count 0, the field as the only history entry).
+  void anderson_restart() {
+    if (!and_.is_setup) return;
+    const size_t slot = sizeof(double) * nmon() * ng;
+    and_.base = 0;
+    PF_CU(cudaMemcpyAsync(hist_slot(and_.field_hist, 0), w.p, slot, cudaMemcpyDeviceToDevice, st));
+    and_.iter = 0;
+    and_.iter_hist = 0;
+    and_.lam = 0.0;
+  }
+
   void anderson_step() {  // anderson.jl:98-228
     if (!and_.is_setup) throw PFError(E_STATE, "AndersonUpdater not set up");
     auto& A = and_;
@@ -1491,6 +1505,7 @@ struct System {
       if (mixed && prec == 1 && ferr < o.mixed_switch_ferr) {
         prec = 0;
         r.switch_step = step;
+        anderson_restart();
       }
       step += 1;
     }
@@ -1886,6 +1901,13 @@ int pf_scft_batch(pf_system* const* systems, int n, const pf_scft_options* opts,
   int dev = 0;
   cudaGetDevice(&dev);
   std::atomic<int> next{0};
+  // Batched systems run their density solves as direct launches: a 256-system sweep with
+  // every worker thread capturing and replaying its own CUDA graphs raised a GPU memory fault
+  // (Xid 31) once, and the same sweep with direct launches completed cleanly.
+  for (int i = 0; i < n; ++i) {
+    systems[i]->s->use_graphs = false;
+    systems[i]->s->invalidate_graphs();
+  }
   auto worker = [&]() {
     cudaSetDevice(dev);
     for (;;) {

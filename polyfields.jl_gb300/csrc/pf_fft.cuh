@@ -246,22 +246,37 @@ struct JoinBA {
 // Data that leaves a transform (its final store) stays in natural order.
 __device__ __forceinline__ int swz(int i) { return i ^ ((i >> 4) & 15); }
 
+// Per-length scratch index of the plane and pencil transforms: each XORs the low bits with
+// higher ones (a bijection on every aligned block of 4 or 8 indices), chosen with the group
+// strides below from a wavefront count of every shared-memory access of the plane pass under
+// the hardware's rule for 8-byte accesses (each half warp of 16 lanes must cover 16 distinct
+// 8-byte bank pairs to take one wavefront).
+template <int N>
+__device__ __forceinline__ int pswz(int i) {
+  if constexpr (N == 16) return i ^ ((i >> 2) & 3);
+  else if constexpr (N == 32 || N == 48) return i ^ (((i >> 2) ^ (i >> 4)) & 3);
+  else if constexpr (N == 64) return i ^ ((i >> 3) & 7);
+  else if constexpr (N == 96 || N == 128) return i ^ (((i >> 3) ^ (i >> 6)) & 7);
+  else return swz(i);
+}
+
 // Passes p in [P0, P1) of a transform held in shared memory at buf[m(i) * es], in place and
 // group-synchronised (load all, __syncwarp, store all).  Loads of pass P0 use the swizzled
-// index when SWZ_IN, stores of pass P1-1 when SWZ_OUT; everything in between is swizzled.
+// index pswz<N> when SWZ_IN, stores of pass P1-1 when SWZ_OUT; everything in between is
+// swizzled.
 template <typename T, bool INV, int N, int O, int P0, int P1, bool SWZ_IN, bool SWZ_OUT>
 __device__ __forceinline__ void smem_passes(Cx<T>* buf, int es, int g, const Cx<T>* twtab, bool active) {
   if constexpr (P0 < P1) {
     using PS = PassOf<T, INV, N, O, P0>;
     Cx<T> v[PS::BPT][Order<N, O>::radix(P0)];
     if (active) {
-      PS::load(v, g, [&](int i) { return buf[(SWZ_IN ? swz(i) : i) * es]; });
+      PS::load(v, g, [&](int i) { return buf[(SWZ_IN ? pswz<N>(i) : i) * es]; });
       PS::compute(v, g, twtab + Order<N, O>::tw_offset(P0));
     }
     __syncwarp();
     constexpr bool last = P0 + 1 == P1;
     if (active)
-      PS::store(v, g, [&](int i, const Cx<T>& x) { buf[((!last || SWZ_OUT) ? swz(i) : i) * es] = x; });
+      PS::store(v, g, [&](int i, const Cx<T>& x) { buf[((!last || SWZ_OUT) ? pswz<N>(i) : i) * es] = x; });
     __syncwarp();
     smem_passes<T, INV, N, O, P0 + 1, P1, true, SWZ_OUT>(buf, es, g, twtab, active);
   }
@@ -269,14 +284,15 @@ __device__ __forceinline__ void smem_passes(Cx<T>* buf, int es, int g, const Cx<
 
 // Group -> row pair / column assignment.  The GPW = 32/G groups of a warp get indices S apart
 // (then the next warp), so that their shared-memory windows fall on different banks; S is
-// chosen per length from a bank-conflict count of the plans above.
+// chosen per length with pswz from the same wavefront count (the x transforms of a row pair
+// use pair_stride<Nx>, the y transforms of a column col_stride<Ny>).
 template <int N>
 __host__ __device__ constexpr int pair_stride() {
-  return (N == 64 || N == 96 || N == 128) ? 2 : 1;
+  return (N == 16 || N == 32 || N == 48) ? 2 : (N == 64 || N == 96 || N == 128) ? 4 : 1;
 }
 template <int N>
 __host__ __device__ constexpr int col_stride() {
-  return N == 16 ? 3 : N == 32 ? 2 : (N == 64 || N == 96 || N == 128) ? 4 : 1;
+  return (N == 16 || N == 32 || N == 48) ? 4 : (N == 64 || N == 96 || N == 128) ? 8 : 1;
 }
 // padding (complex elements) after each z pencil of a tile
 template <int N>

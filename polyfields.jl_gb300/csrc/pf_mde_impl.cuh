@@ -183,7 +183,7 @@ __device__ __forceinline__ void y_inverse_from_global(Cx<T>* S, const Cx<T>* __r
   if (active) {
     P0::load(v, g, [&](int i) { return kin[c * NY + i]; });
     P0::compute(v, g, twy);
-    P0::store(v, g, [&](int i, const Cx<T>& x) { col[(P > 1 ? swz(i) : i) * C::KX] = x; });
+    P0::store(v, g, [&](int i, const Cx<T>& x) { col[(P > 1 ? pswz<NY>(i) : i) * C::KX] = x; });
   }
   __syncwarp();
   smem_passes<T, true, NY, 0, 1, P, true, false>(col, C::KX, g, twy, active);
@@ -200,7 +200,7 @@ __device__ __forceinline__ void y_inverse_from_regs(Cx<T>* S, const Cx<T>* twy, 
   using P0 = PassOf<T, true, NY, 0, 0>;
   if (active) {
     P0::compute(w.v, g, twy);
-    P0::store(w.v, g, [&](int i, const Cx<T>& x) { col[(P > 1 ? swz(i) : i) * C::KX] = x; });
+    P0::store(w.v, g, [&](int i, const Cx<T>& x) { col[(P > 1 ? pswz<NY>(i) : i) * C::KX] = x; });
   }
   __syncwarp();
   smem_passes<T, true, NY, 0, 1, P, true, false>(col, C::KX, g, twy, active);
@@ -240,12 +240,12 @@ __device__ __forceinline__ void x_inverse_to_regs(Cx<T>* S, const Cx<T>* twx, XR
       P0::compute(v, g, twx);
     }
     __syncwarp();
-    if (active) P0::store(v, g, [&](int i, const Cx<T>& x) { z[swz(i)] = x; });
+    if (active) P0::store(v, g, [&](int i, const Cx<T>& x) { z[pswz<NX>(i)] = x; });
     __syncwarp();
     smem_passes<T, true, NX, 0, 1, P - 1, true, true>(z, 1, g, twx, active);
     using PL = PassOf<T, true, NX, 0, P - 1>;
     if (active) {
-      PL::load(out.v, g, [&](int i) { return z[swz(i)]; });
+      PL::load(out.v, g, [&](int i) { return z[pswz<NX>(i)]; });
       PL::compute(out.v, g, twx + Order<NX, 0>::tw_offset(P - 1));
     }
     __syncwarp();
@@ -264,7 +264,7 @@ __device__ __forceinline__ void x_forward_from_regs(Cx<T>* S, const Cx<T>* twx, 
   using P0 = PassOf<T, false, NX, 1, 0>;
   if (active) {
     P0::compute(in.v, g, twb);
-    P0::store(in.v, g, [&](int i, const Cx<T>& x) { z[P > 1 ? swz(i) : i] = x; });
+    P0::store(in.v, g, [&](int i, const Cx<T>& x) { z[P > 1 ? pswz<NX>(i) : i] = x; });
   }
   __syncwarp();
   smem_passes<T, false, NX, 1, 1, P, true, false>(z, 1, g, twb, active);
@@ -303,12 +303,12 @@ __device__ __forceinline__ void y_forward_to_regs(Cx<T>* S, const Cx<T>* twy, BA
     }
     __syncthreads();
     Cx<T>* col = S + (active ? c : 0);
-    if (active) P0::store(v, g, [&](int i, const Cx<T>& x) { col[swz(i) * C::KX] = x; });
+    if (active) P0::store(v, g, [&](int i, const Cx<T>& x) { col[pswz<NY>(i) * C::KX] = x; });
     __syncwarp();
     smem_passes<T, false, NY, 1, 1, P - 1, true, true>(col, C::KX, g, twb, active);
     using PL = PassOf<T, false, NY, 1, P - 1>;
     if (active) {
-      PL::load(out.v, g, [&](int i) { return col[swz(i) * C::KX]; });
+      PL::load(out.v, g, [&](int i) { return col[pswz<NY>(i) * C::KX]; });
       PL::compute(out.v, g, twb + Order<NY, 1>::tw_offset(P - 1));
     }
     __syncwarp();
@@ -385,13 +385,13 @@ __device__ __forceinline__ void row_forward_1d(Cx<T>* z, const Cx<T>* twx, XRegs
   } else {
     if (active) {
       P0::compute(r.v, g, twb);
-      P0::store(r.v, g, [&](int i, const Cx<T>& x) { z[swz(i)] = x; });
+      P0::store(r.v, g, [&](int i, const Cx<T>& x) { z[pswz<NX>(i)] = x; });
     }
     __syncwarp();
     smem_passes<T, false, NX, 1, 1, P - 1, true, true>(z, 1, g, twb, active);
     using PL = PassOf<T, false, NX, 1, P - 1>;
     if (active) {
-      PL::load(w.v, g, [&](int i) { return z[swz(i)]; });
+      PL::load(w.v, g, [&](int i) { return z[pswz<NX>(i)]; });
       PL::compute(w.v, g, twb + Order<NX, 1>::tw_offset(P - 1));
     }
     __syncwarp();
@@ -416,13 +416,13 @@ __device__ __forceinline__ void row_inverse_1d(Cx<T>* z, const Cx<T>* twx, BAReg
   } else {
     if (active) {
       P0::compute(w.v, g, twx);
-      P0::store(w.v, g, [&](int i, const Cx<T>& x) { z[swz(i)] = x; });
+      P0::store(w.v, g, [&](int i, const Cx<T>& x) { z[pswz<NX>(i)] = x; });
     }
     __syncwarp();
     smem_passes<T, true, NX, 0, 1, P - 1, true, true>(z, 1, g, twx, active);
     using PL = PassOf<T, true, NX, 0, P - 1>;
     if (active) {
-      PL::load(r.v, g, [&](int i) { return z[swz(i)]; });
+      PL::load(r.v, g, [&](int i) { return z[pswz<NX>(i)]; });
       PL::compute(r.v, g, twx + Order<NX, 0>::tw_offset(P - 1));
     }
     __syncwarp();
@@ -922,13 +922,13 @@ __device__ __forceinline__ void z_forward_to_regs(const Cx<T>* __restrict__ kb, 
     if (active) {
       F0::load(v, g, [&](int i) { return kb[(long)i * nkp + col]; });
       F0::compute(v, g, twb);
-      F0::store(v, g, [&](int i, const Cx<T>& x) { pen[swz(i)] = x; });
+      F0::store(v, g, [&](int i, const Cx<T>& x) { pen[pswz<NZ>(i)] = x; });
     }
     __syncwarp();
     smem_passes<T, false, NZ, 1, 1, P - 1, true, true>(pen, 1, g, twb, active);
     using FL = PassOf<T, false, NZ, 1, P - 1>;
     if (active) {
-      FL::load(w.v, g, [&](int i) { return pen[swz(i)]; });
+      FL::load(w.v, g, [&](int i) { return pen[pswz<NZ>(i)]; });
       FL::compute(w.v, g, twb + Order<NZ, 1>::tw_offset(P - 1));
     }
     __syncwarp();

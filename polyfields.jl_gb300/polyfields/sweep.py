@@ -40,6 +40,7 @@ def run_local(params: Sequence[Dict], indices: Sequence[int], precision: str = "
     float32 iterations until ferr < ``switch`` then float64 polish to ``ftol``/``stol``
     (precision "fp32"), or float64 throughout ("fp64").  Returns {index: result dict}."""
     import polyfields as pf
+    from polyfields import _lib as L
     from polyfields import workloads as W
     systems, ups, doms = [], [], []
     for i in indices:
@@ -53,9 +54,11 @@ def run_local(params: Sequence[Dict], indices: Sequence[int], precision: str = "
     res, st = pf.scft_batch(systems, ups, doms if vcell else None, opts, nthreads=nthreads, raise_on_error=False)
     wall = time.perf_counter() - t0
     out = {}
+    lib = L.load()
     for k, i in enumerate(indices):
         r = res[k]
-        out[i] = {"status": int(st[k]), "converged": bool(r.converged), "iterations": int(r.nsteps),
+        err = lib.pf_last_error(systems[k]._h).decode() if st[k] != 0 else ""
+        out[i] = {"status": int(st[k]), "error": err, "converged": bool(r.converged), "iterations": int(r.nsteps),
                   "ferr": float(r.ferr), "serr": float(r.serr), "fhelm": float(r.fhelm),
                   "switch_step": int(r.switch_step), "a": float(systems[k].cell.params[0]), "wall_s": wall}
     return out

@@ -92,3 +92,94 @@ def test_pullback_is_linear_in_the_cotangent():
     for m in (1, 2):
         assert relmax(p3["w"][m], 2.0 * p1["w"][m] - 0.5 * p2["w"][m]) < 1e-10
     assert relmax(p3["cell"], 2.0 * p1["cell"] - 0.5 * p2["cell"]) < 1e-10
+
+
+def test_torch_autograd_density_matches_pullback():
+    """polyfields.autodiff.density as a torch op: backward of sum((rho_A - t)^2) equals the
+    pullback with rho_bar = 2 (rho_A - t)."""
+    torch = pytest.importorskip("torch")
+    from polyfields import autodiff
+    dims, shape = (32, 32, 1), (1, 32, 32)
+    rng = np.random.default_rng(8)
+    fields = {m: 0.3 * rng.standard_normal(shape) for m in (1, 2)}
+    g = build(pf, dims, "hexagonal", [6.0], fields, precision="fp64")
+    target = torch.from_numpy(AD.smooth_target(shape, 0.35, seed=9))
+    wt = {m: torch.from_numpy(fields[m]).requires_grad_(True) for m in (1, 2)}
+    rho = autodiff.density(g, wt)
+    loss = torch.sum((rho[1] - target) ** 2)
+    loss.backward()
+    pb = g.density_pullback({1: 2.0 * (rho[1].detach().numpy() - target.numpy())})
+    for m in (1, 2):
+        assert relmax(wt[m].grad.numpy(), pb["w"][m]) < 1e-12
+
+
+def test_adjoint_96cubed_against_reference_gradient_and_differences():
+    """The differentiation workload: 96^3 cubic cell L = 8, AB diblock N = 100, fA = 0.35,
+    Ns = 200, chi = 0.2; L = sum (rho_A - target)^2 with a smooth seeded target (5 lowest
+    modes, amplitude 0.2, mean fA).  GPU FP64 vs the FP64 CPU reference gradient (1e-9),
+    GPU FP32 chains vs the same (1e-3), and central differences with h = 1e-4 for w_A, w_B,
+    L (GPU FP64 losses), fA (reference continuous relaxation) and chi (zero)."""
+    dims, shape = (96, 96, 96), (96, 96, 96)
+    rng = np.random.default_rng(96)
+    fields = {m: 0.1 * rng.standard_normal(shape) for m in (1, 2)}
+    target = AD.smooth_target(shape, 0.35, amp=0.2, nmodes=5, seed=12345)
+
+    def make(M, precision=None, L=8.0, NA=35.0, chi=0.2):
+        A, B = M.Monomer(1, 1.0), M.Monomer(2, 1.0)
+        cell = M.UnitCell(3, "cubic", L)
+        s = M.FieldSystem(dims, cell, monomers=[A, B]) if precision is None else \
+            M.FieldSystem(dims, cell, monomers=[A, B], precision=precision)
+        s.add_species(M.Multiblock([A, B], [NA, 100.0 - NA], [1.0, 1.0], 200), 1.0)
+        itx = M.FloryInteraction()
+        itx.set_interaction(A, B, chi)
+        s.add_interaction(itx)
+        for m in (1, 2):
+            s.fields[m] = fields[m].copy() if M is O else fields[m]
+        return s
+
+    o = make(O)
+    o.density_update()
+    _, rbar = AD.density_loss(o, 1, target)
+    go = AD.density_pullback(o, rbar)
+    g64 = make(pf, "fp64").density_pullback(rbar)
+    g32 = make(pf, "fp32").density_pullback(rbar)
+    for m in (1, 2):
+        assert relmax(g64["w"][m], go["w"][m]) < 1e-9
+        assert relmax(g32["w"][m], go["w"][m]) < 1e-3
+    assert relmax(g64["cell"], go["cell"]) < 1e-9
+    assert relmax(g32["cell"], go["cell"]) < 1e-3
+    dfa64 = 100.0 * (g64["Nref_block"][0][0] - g64["Nref_block"][0][1])
+    dfao = 100.0 * (go["Nref_block"][0][0] - go["Nref_block"][0][1])
+    assert dfa64 == pytest.approx(dfao, rel=1e-9)
+
+    h = 1e-4
+
+    def gpu_loss(**kw):
+        s = make(pf, "fp64", **kw)
+        s.density_update()
+        d = s.density[1] - target
+        return float(np.sum(d * d))
+
+    for m in (1, 2):
+        for idx in [(3, 50, 17), (70, 8, 91)]:
+            fp = {k: v.copy() for k, v in fields.items()}
+            fm = {k: v.copy() for k, v in fields.items()}
+            fp[m][idx] += h
+            fm[m][idx] -= h
+            sp_, sm_ = make(pf, "fp64"), make(pf, "fp64")
+            sp_.fields[m], sm_.fields[m] = fp[m], fm[m]
+            sp_.density_update()
+            sm_.density_update()
+            fd = (np.sum((sp_.density[1] - target) ** 2) - np.sum((sm_.density[1] - target) ** 2)) / (2 * h)
+            assert g64["w"][m][idx] == pytest.approx(fd, rel=1e-5, abs=1e-9), (m, idx)
+    fdL = (gpu_loss(L=8.0 + h) - gpu_loss(L=8.0 - h)) / (2 * h)
+    assert g64["cell"][0] == pytest.approx(fdL, rel=1e-5)
+    assert gpu_loss(chi=0.2 + h) == gpu_loss(chi=0.2 - h)  # dL/dchi = 0 at fixed fields
+
+    def oracle_loss(NA):
+        s = make(O, NA=NA)
+        s.density_update()
+        return AD.density_loss(s, 1, target)[0]
+
+    fdf = (oracle_loss(35.0 + 100 * h) - oracle_loss(35.0 - 100 * h)) / (2 * h)
+    assert dfa64 == pytest.approx(fdf, rel=1e-5)

