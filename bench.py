@@ -224,13 +224,17 @@ def run_gpu(args):
     ferr = sysm.field_error()
     fhelm = sysm.free_energy()
 
-    # ---- roofline of the dominant kernel pair (one MDE contour step: xy_step + z_step)
+    # ---- roofline of the dominant kernel pair (one MDE contour step: xy_step + z_pipe)
     peak, peak_kind = measured_peaks()
     alg_bytes = 3 * 4 * ng  # read q_s (f32), read LW (f32), write q_{s+1} (f32)
     achieved = alg_bytes / (mde_step_us * 1e-6) / 1e9
-    roofline = {"bound": "hbm", "kernel": "MDE contour step (xy_step_kernel<float,128,128> + z_step_kernel<float,128>)",
+    # DRAM bytes of one contour step of one chain at 128^3 (xy_step + z_pipe launches) from an
+    # ncu capture of the large blend with Ns = 20 (profile_mde.py --blend): reads 16.96 MB +
+    # 12.82 MB, writes 0 (absorbed by L2 within the launch); cold caches.
+    traffic = 29.78e6 if n == 128 else None
+    roofline = {"bound": "hbm", "kernel": "MDE contour step (xy_step_kernel<float,128,128> + z_pipe_kernel<float,128>)",
                 "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_launch": alg_bytes,
+                "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
                 "avg_step_us": mde_step_us}
 
     # ---- e2e through the public API with host buffers (pinned when torch is present)
