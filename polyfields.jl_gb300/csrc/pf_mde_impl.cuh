@@ -330,18 +330,18 @@ __device__ __forceinline__ void finish_regs(XRegs<T, NX>& r, int p, int g, const
     for (int t = 0; t < J::R; ++t) {
       const int x = J::pos(g, b, t);
       const int i0 = y0 * NX + x, i1 = y1 * NX + x;
-      const T l0 = lw_cur[i0];
+      const T l0 = __ldg(lw_cur + i0);
       const T q0 = l0 * (r.v[b][t].x * cs);
-      qout[i0] = q0;
+      __stcs(qout + i0, q0);  // history: streamed past L2, which keeps LW and the spectra
       T l1 = (T)0, q1 = (T)0;
       if constexpr (NY > 1) {
-        l1 = lw_cur[i1];
+        l1 = __ldg(lw_cur + i1);
         q1 = l1 * (r.v[b][t].y * cs);
-        qout[i1] = q1;
+        __stcs(qout + i1, q1);
       }
       if (lw_next) {
-        const T n0 = same ? l0 : lw_next[i0];
-        const T n1 = NY > 1 ? (same ? l1 : lw_next[i1]) : (T)0;
+        const T n0 = same ? l0 : __ldg(lw_next + i0);
+        const T n1 = NY > 1 ? (same ? l1 : __ldg(lw_next + i1)) : (T)0;
         r.v[b][t] = cx<T>(n0 * q0, n1 * q1);
       }
     }
