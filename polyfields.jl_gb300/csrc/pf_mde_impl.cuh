@@ -725,6 +725,7 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
     fence_mbar_init();
   }
   __syncthreads();
+  const uint64_t keep = l2_evict_last();  // LD is read by every step of the chain's block
   auto issue = [&](int k) {  // thread 0: fill stage k % S with round k of this CTA
     const int s = k % S, r = (int)blockIdx.x + k * (int)gridDim.x;
     const int nt = min(TPC, ntiles - r * TPC);
@@ -732,7 +733,8 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
     for (int j = 0; j < nt; ++j) {
       const int tile = r * TPC + j;
       tma_load_2d(ktiles + (size_t)(s * TPC + j) * (Z::KB / Z::E), &kmap, tile * 16, 0, &full[s]);
-      tma_load_2d(ltiles + (size_t)(s * TPC + j) * (Z::LB / sizeof(T)), &lmap, tile * Z::M, 0, &full[s]);
+      tma_load_2d_hint(ltiles + (size_t)(s * TPC + j) * (Z::LB / sizeof(T)), &lmap, tile * Z::M, 0, &full[s],
+                       keep);
     }
   };
   if (threadIdx.x == 0)
