@@ -2,6 +2,10 @@
 
     python polyfields.jl_gb300/converge.py [--n 128] [--nsteps 4000] [--switch 1e-5] [--modes mixed,fp64]
         [--nhist 20] [--iter-euler 1] [--lam-euler 0.01] [--nskip 5] [--nper 20] [--fixed-cell]
+        [--system blend|bcc]
+
+--system bcc runs the 3D BCC workload instead (AB diblock fA 0.3, N100, Ns 100, cubic L0 7,
+twelve {110} cosines + 0.1 noise).
 
 Builds the large blend (AB diblock N100 fA0.4 at phi 0.8 + A homopolymer N50 at phi 0.2,
 chi 0.2, Ns 200, cubic cell L0 = 14, double-gyroid start plus 0.05 seeded noise) on an n^3
@@ -23,7 +27,10 @@ from polyfields import workloads as W  # noqa: E402
 
 
 def run(n, precision, nsteps, switch, ftol, stol, nsout, a):
-    sysm = W.blend3d_system(pf, n=n, precision=precision)
+    if a.system == "bcc":
+        sysm = W.bcc_system(pf, n=n, precision=precision)
+    else:
+        sysm = W.blend3d_system(pf, n=n, precision=precision)
     sysm.synchronize()
     opts = pf.SCFTOptions(nsteps=nsteps, ftol=ftol, stol=stol, nsout=nsout,
                           mixed_switch_ferr=switch if precision == "fp32" else 0.0)
@@ -53,9 +60,11 @@ def main():
     ap.add_argument("--nskip", type=int, default=5)
     ap.add_argument("--nper", type=int, default=20)
     ap.add_argument("--fixed-cell", action="store_true", help="no DomainUpdater (cell held at L0)")
+    ap.add_argument("--system", default="blend", choices=["blend", "bcc"])
     a = ap.parse_args()
-    cellmode = "fixed cell L0 = 14" if a.fixed_cell else f"DomainUpdater nskip {a.nskip} nper {a.nper}"
-    out = {"workload": f"large blend {a.n}^3, Ns 200, Anderson nhist {a.nhist} (iter_euler {a.iter_euler}, "
+    cellmode = "fixed cell" if a.fixed_cell else f"DomainUpdater nskip {a.nskip} nper {a.nper}"
+    name = "large blend" if a.system == "blend" else "BCC diblock fA0.3 L0 7, Ns 100"
+    out = {"workload": f"{name} {a.n}^3, Anderson nhist {a.nhist} (iter_euler {a.iter_euler}, "
                        f"lam_euler {a.lam_euler}), {cellmode}", "ftol": a.ftol, "stol": a.stol,
            "switch_ferr": a.switch, "runs": []}
     for mode in a.modes.split(","):

@@ -130,3 +130,26 @@ def hex_instance(M, n, chi, NA, a0, seed, precision=None, Ns=100, scale=0.1, amp
     six = amp * (np.cos(2 * np.pi * x) + np.cos(2 * np.pi * y) + np.cos(2 * np.pi * (x + y)))
     M.fieldinit(sys, seeded_fields(shape, [1, 2], seed, scale, six))
     return sys
+
+
+def bcc_system(M, n=64, L=7.0, precision=None, Ns=100, seed=12345):
+    """The 3D BCC workload: AB diblock N100 fA0.30 (built as Multiblock([A, B], [30, 70])),
+    chi 0.2, Ns 100, cubic cell L0; w_A = 0.1 N(0,1) + the sum of cos(2 pi h.r / L) over the 12
+    {110} reflections (h = (+-1, +-1, 0) and permutations; fractional coordinates on the
+    grid) scaled to amplitude 1.0 (the raw sum peaks at 12, which as a field would overflow
+    the propagators), w_B = -w_A."""
+    A, B = M.Monomer(1), M.Monomer(2)
+    sys = _fs(M, (n, n, n), M.UnitCell(3, "cubic", L), [A, B], precision)
+    sys.add_species(M.Multiblock([A, B], [30, 70], [1.0, 1.0], Ns), 1.0)
+    itx = M.FloryInteraction()
+    itx.set_interaction(A, B, 0.2)
+    sys.add_interaction(itx)
+    shape = (n, n, n)
+    z, y, x = np.meshgrid(*(np.arange(n) / n for _ in range(3)), indexing="ij")
+    pat = np.zeros(shape)
+    for a, b in ((x, y), (y, z), (z, x)):  # 6 +-pairs x 2 signs = 12 reflections
+        pat += 2.0 * np.cos(2 * np.pi * (a + b)) + 2.0 * np.cos(2 * np.pi * (a - b))
+    rng = np.random.Generator(np.random.PCG64(seed))
+    wa = 0.1 * rng.standard_normal(shape) + pat / 12.0
+    M.fieldinit(sys, {1: wa, 2: -wa})
+    return sys
