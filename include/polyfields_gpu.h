@@ -133,6 +133,17 @@ int pf_anderson_create(pf_system* sys, int nhist, int iter_euler, double lam_eul
 int pf_anderson_setup(pf_system* sys);
 /* step!(::AndersonUpdater) (src/updaters/anderson.jl:98-228) */
 int pf_anderson_step(pf_system* sys);
+/* EulerUpdater(; method = :PECE, lam = 0.05) (src/updaters/euler.jl:9-29): method 0 = :PEC,
+ * 1 = :PECE.  Becomes the handle's field updater (replacing an AndersonUpdater). */
+int pf_euler_create(pf_system* sys, int method, double lam);
+/* MomentumUpdater(; method = :MOM, lam = 0.01, gamma = 0.9, beta1 = 0.9, beta2 = 0.999)
+ * (src/updaters/momentum.jl:19-47): method 0 = :MOM, 1 = :RMS, 2 = :ADAM, 3 = :NAG.  Becomes
+ * the handle's field updater. */
+int pf_momentum_create(pf_system* sys, int method, double lam, double gamma, double beta1, double beta2);
+/* setup!(updater, sys) / step!(updater) for the field updater created last (Anderson, Euler
+ * or Momentum): src/updaters/base.jl:7-9 dispatch. */
+int pf_updater_setup(pf_system* sys);
+int pf_updater_step(pf_system* sys);
 /* DomainUpdater(; nper = 10, nskip = 200, lam = 0.1, pmax = 1.0, rlxn = 0.5) (src/updaters/domain.jl:20-24) */
 int pf_domain_create(pf_system* sys, int nper, int nskip, double lam, double pmax, double rlxn);
 /* setup!(::DomainUpdater, sys) (src/updaters/domain.jl:32-42): computes the stress. */
@@ -142,8 +153,9 @@ int pf_domain_step(pf_system* sys, int nsteps);
 /* stress_error(domain) (src/updaters/domain.jl:30) */
 int pf_domain_stress_error(pf_system* sys, double* out);
 
-/* scft!(sys, AndersonUpdater; domain, opts) (src/simulate.jl:60-148) with the updaters created
- * by pf_anderson_create (required) and pf_domain_create (used when use_domain != 0). */
+/* scft!(sys, updater; domain, opts) (src/simulate.jl:60-148) with the field updater created
+ * last (pf_anderson_create, pf_euler_create or pf_momentum_create; required) and the
+ * DomainUpdater of pf_domain_create (used when use_domain != 0). */
 int pf_scft(pf_system* sys, const pf_scft_options* opts, int use_domain, pf_scft_results* out);
 
 /* ---- pullback of density! (no counterpart in the reference: PolyFields.jl has no derivatives) ----

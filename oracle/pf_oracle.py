@@ -1078,6 +1078,63 @@ class EulerUpdater:
             sys.residuals_update()
 
 
+class MomentumUpdater:
+    """src/updaters/momentum.jl:19-165: MOM (first-moment average with beta1), RMS (second
+    moment with beta2, step r / (sqrt(v) + 1e-8)), ADAM (both, no bias correction) and NAG
+    (look-ahead gradient with gamma); every method ends with w += lam * step."""
+
+    def __init__(self, method: str = "MOM", lam: float = 0.01, gamma: float = 0.9, beta1: float = 0.9,
+                 beta2: float = 0.999):
+        assert 0.0 < gamma < 1.0 and 0.0 < beta1 < 1.0 and 0.0 < beta2 < 1.0
+        if method not in ("MOM", "RMS", "ADAM", "NAG"):
+            raise ValueError("Invalid `method` parameter for MomentumUpdater. Options include: (:MOM, :RMS, :ADAM, :NAG)")
+        self.method = method
+        self.lam, self.gamma, self.beta1, self.beta2 = float(lam), float(gamma), float(beta1), float(beta2)
+        self.system = None
+
+    def setup(self, sys):
+        self.system = sys
+        self.stepv = {mid: r.copy() for mid, r in sys.residuals.items()}
+        self.temp = {mid: w.copy() for mid, w in sys.fields.items()}
+        self.mt = {mid: np.zeros(sys.shape) for mid in sys.fields}
+        self.vt = {mid: np.zeros(sys.shape) for mid in sys.fields}
+
+    def step(self):
+        sys = self.system
+        b1, b2, g = self.beta1, self.beta2, self.gamma
+        if self.method == "MOM":
+            sys.residuals_update()
+            for mid in self.mt:
+                self.mt[mid] = b1 * self.mt[mid] + (1 - b1) * sys.residuals[mid]
+            self.stepv = {mid: m.copy() for mid, m in self.mt.items()}
+        elif self.method == "RMS":
+            sys.residuals_update()
+            for mid in self.vt:
+                self.vt[mid] = b2 * self.vt[mid] + (1 - b2) * sys.residuals[mid] ** 2
+            for mid in self.stepv:
+                self.stepv[mid] = sys.residuals[mid] / (np.sqrt(self.vt[mid]) + 1e-8)
+        elif self.method == "ADAM":
+            sys.residuals_update()
+            for mid in self.mt:
+                self.mt[mid] = b1 * self.mt[mid] + (1 - b1) * sys.residuals[mid]
+            for mid in self.vt:
+                self.vt[mid] = b2 * self.vt[mid] + (1 - b2) * sys.residuals[mid] ** 2
+            for mid in self.stepv:
+                self.stepv[mid] = self.mt[mid] / (np.sqrt(self.vt[mid]) + 1e-8)
+        else:  # NAG
+            self.temp = {mid: w.copy() for mid, w in sys.fields.items()}
+            for mid in sys.fields:
+                sys.fields[mid] = sys.fields[mid] + self.lam * self.mt[mid]
+            sys.residuals_update()
+            for mid in self.mt:
+                self.mt[mid] = g * self.mt[mid] + (1 - g) * sys.residuals[mid]
+            self.stepv = {mid: m.copy() for mid, m in self.mt.items()}
+            for mid in sys.fields:
+                sys.fields[mid] = self.temp[mid].copy()
+        for mid in sys.fields:
+            sys.fields[mid] = sys.fields[mid] + self.lam * self.stepv[mid]
+
+
 class DomainUpdater:
     """src/updaters/domain.jl:7-121 (quirk Q4)."""
 

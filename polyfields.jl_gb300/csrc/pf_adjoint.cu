@@ -1,4 +1,5 @@
-// Elementwise and reduction pieces of the adjoint (pullback) of density!.
+// Elementwise and reduction pieces of the adjoint (pullback) of density!, and the Euler and
+// momentum field updaters (elementwise, at the end of this file).
 //
 // The reference has no derivative code.  These kernels serve the hand-derived adjoint of
 // the chain propagation (src/species/multiblock.jl:125-231): for every application
@@ -151,5 +152,92 @@ void launch_ddot(const double* a, const double* b, long n, double* part, double*
   template void launch_adj_init<T>(T*, const AdjSrc<T>&, double, long, cudaStream_t);
 PF_ADJ_INST(float)
 PF_ADJ_INST(double)
+
+}  // namespace pf
+
+// ------------------------------------------------------------------ Euler and momentum updaters
+// src/updaters/euler.jl:36-65 and src/updaters/momentum.jl:63-165, elementwise over all
+// monomer grids (n = nmon * Ng).
+namespace pf {
+
+// predictor: w += lam r; temp = w + lam/2 r (on the updated w, as the reference does)
+__global__ void euler_predict_kernel(double* __restrict__ w, double* __restrict__ temp, const double* __restrict__ r,
+                                     double lam, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double v = w[i] + lam * r[i];
+    w[i] = v;
+    temp[i] = v + 0.5 * lam * r[i];
+  }
+}
+// corrector: w = temp + lam/2 r(w_predicted)
+__global__ void euler_correct_kernel(double* __restrict__ w, const double* __restrict__ temp,
+                                     const double* __restrict__ r, double lam, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    w[i] = temp[i] + 0.5 * lam * r[i];
+}
+// MOM (0), RMS (1), ADAM (2): moments from the fresh residual, then w += lam * step
+__global__ void momentum_kernel(int method, double* __restrict__ w, double* __restrict__ m, double* __restrict__ v,
+                                const double* __restrict__ r, double lam, double b1, double b2, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double ri = r[i];
+    double step;
+    if (method == 0) {
+      const double mi = b1 * m[i] + (1.0 - b1) * ri;
+      m[i] = mi;
+      step = mi;
+    } else if (method == 1) {
+      const double vi = b2 * v[i] + (1.0 - b2) * ri * ri;
+      v[i] = vi;
+      step = ri / (sqrt(vi) + 1e-8);
+    } else {
+      const double mi = b1 * m[i] + (1.0 - b1) * ri;
+      const double vi = b2 * v[i] + (1.0 - b2) * ri * ri;
+      m[i] = mi;
+      v[i] = vi;
+      step = mi / (sqrt(vi) + 1e-8);
+    }
+    w[i] += lam * step;
+  }
+}
+// NAG look-ahead: temp = w; w += lam m
+__global__ void nag_ahead_kernel(double* __restrict__ w, double* __restrict__ temp, const double* __restrict__ m,
+                                 double lam, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    temp[i] = w[i];
+    w[i] += lam * m[i];
+  }
+}
+// NAG update: m = gamma m + (1 - gamma) r(look-ahead); w = temp + lam m
+__global__ void nag_update_kernel(double* __restrict__ w, const double* __restrict__ temp, double* __restrict__ m,
+                                  const double* __restrict__ r, double lam, double gamma, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double mi = gamma * m[i] + (1.0 - gamma) * r[i];
+    m[i] = mi;
+    w[i] = temp[i] + lam * mi;
+  }
+}
+
+void launch_euler_predict(double* w, double* temp, const double* r, double lam, long n, cudaStream_t st) {
+  euler_predict_kernel<<<adj_blocks(n), 256, 0, st>>>(w, temp, r, lam, n);
+  count_launches(1);
+}
+void launch_euler_correct(double* w, const double* temp, const double* r, double lam, long n, cudaStream_t st) {
+  euler_correct_kernel<<<adj_blocks(n), 256, 0, st>>>(w, temp, r, lam, n);
+  count_launches(1);
+}
+void launch_momentum(int method, double* w, double* m, double* v, const double* r, double lam, double b1, double b2,
+                     long n, cudaStream_t st) {
+  momentum_kernel<<<adj_blocks(n), 256, 0, st>>>(method, w, m, v, r, lam, b1, b2, n);
+  count_launches(1);
+}
+void launch_nag_ahead(double* w, double* temp, const double* m, double lam, long n, cudaStream_t st) {
+  nag_ahead_kernel<<<adj_blocks(n), 256, 0, st>>>(w, temp, m, lam, n);
+  count_launches(1);
+}
+void launch_nag_update(double* w, const double* temp, double* m, const double* r, double lam, double gamma, long n,
+                       cudaStream_t st) {
+  nag_update_kernel<<<adj_blocks(n), 256, 0, st>>>(w, temp, m, r, lam, gamma, n);
+  count_launches(1);
+}
 
 }  // namespace pf

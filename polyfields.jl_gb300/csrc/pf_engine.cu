@@ -448,6 +448,26 @@ struct System {
       field_hist.release();
     }
   } and_;
+  // EulerUpdater (kind 1, method 0 PEC / 1 PECE) and MomentumUpdater (kind 2, method 0 MOM,
+  // 1 RMS, 2 ADAM, 3 NAG); `active` is the kind of the updater created last (0 = Anderson)
+  struct SimpleUpdater {
+    int kind = 0, method = 0;
+    bool is_setup = false;
+    double lam = 0.05, gamma = 0.9, beta1 = 0.9, beta2 = 0.999;
+    DevBuf temp, mt, vt;
+    void reset(int k, int m, double l) {
+      kind = k;
+      method = m;
+      lam = l;
+      is_setup = false;
+      gamma = beta1 = 0.9;
+      beta2 = 0.999;
+      temp.release();
+      mt.release();
+      vt.release();
+    }
+  } su;
+  int active = 0;
   // Domain updater (src/updaters/domain.jl:7-24)
   struct Domain {
     bool exists = false, is_setup = false;
@@ -1134,6 +1154,50 @@ struct System {
     and_.is_setup = true;
   }
 
+  // ---------------------------------------------------------------- Euler / Momentum
+  void simple_setup() {  // euler.jl:31-35, momentum.jl:49-61
+    const long nall = (long)nmon() * ng;
+    su.temp.alloc(sizeof(double) * nall);
+    PF_CU(cudaMemcpyAsync(su.temp.p, w.p, sizeof(double) * nall, cudaMemcpyDeviceToDevice, st));
+    if (su.kind == 2) {
+      su.mt.alloc(sizeof(double) * nall);
+      su.vt.alloc(sizeof(double) * nall);
+      PF_CU(cudaMemsetAsync(su.mt.p, 0, su.mt.bytes, st));
+      PF_CU(cudaMemsetAsync(su.vt.p, 0, su.vt.bytes, st));
+    }
+    su.is_setup = true;
+  }
+  void simple_step() {  // euler.jl:37-65, momentum.jl:63-165
+    if (!su.is_setup) throw PFError(E_STATE, "field updater not set up");
+    const long nall = (long)nmon() * ng;
+    double* wp = w.as<double>();
+    double* rp = res.as<double>();
+    double* tp = su.temp.as<double>();
+    if (su.kind == 1) {
+      launch_euler_predict(wp, tp, rp, su.lam, nall, st);
+      residuals();
+      launch_euler_correct(wp, tp, rp, su.lam, nall, st);
+      if (su.method == 1) residuals();
+    } else if (su.method == 3) {
+      launch_nag_ahead(wp, tp, su.mt.as<double>(), su.lam, nall, st);
+      residuals();
+      launch_nag_update(wp, tp, su.mt.as<double>(), rp, su.lam, su.gamma, nall, st);
+    } else {
+      residuals();
+      launch_momentum(su.method, wp, su.mt.as<double>(), su.vt.as<double>(), rp, su.lam, su.beta1, su.beta2, nall,
+                      st);
+    }
+    check_launch();
+  }
+  void updater_setup() {
+    if (active == 0) anderson_setup();
+    else simple_setup();
+  }
+  void updater_step() {
+    if (active == 0) anderson_step();
+    else simple_step();
+  }
+
   // Mixed precision: at the float32 -> float64 switch the history holds residuals with
   // float32 rounding (~1e-7 relative), as large as the differences the float64 phase has to
   // resolve; the history restarts from the current field exactly as setup! starts it
@@ -1462,11 +1526,11 @@ struct System {
     auto t0 = std::chrono::steady_clock::now();
     pf_scft_results r{};
     r.switch_step = -1;
-    if (!and_.exists) throw PFError(E_STATE, "no AndersonUpdater created");
+    if (active == 0 && !and_.exists) throw PFError(E_STATE, "no field updater created");
     if (vcell && !dom.exists) throw PFError(E_STATE, "no DomainUpdater created");
     validate();
     residuals();
-    anderson_setup();
+    updater_setup();
     int step = 0;
     double ferr, fhelm;
     stats(ferr, fhelm);
@@ -1485,7 +1549,7 @@ struct System {
     while (step < o.nsteps && !converged) {
       if (o.nsout > 0 && step % o.nsout == 0)
         printf("Step (%-5d / %5d): ferr = %8e, fhelm = %.5e\n", step, o.nsteps, ferr, fhelm);
-      anderson_step();
+      updater_step();
       if (vcell && step % dom.nskip == 0) {
         dom.stress = scfstress();
         serr = stress_error();
@@ -1505,7 +1569,7 @@ struct System {
       if (mixed && prec == 1 && ferr < o.mixed_switch_ferr) {
         prec = 0;
         r.switch_step = step;
-        anderson_restart();
+        if (active == 0) anderson_restart();
       }
       step += 1;
     }
@@ -1824,12 +1888,43 @@ int pf_anderson_create(pf_system* sys, int nhist, int iter_euler, double lam_eul
     if (nhist < 1 || nhist > 60) throw pf::PFError(PF_EARG, "nhist must be in [1, 60]");
     s.and_.reset();
     s.and_.exists = true;
+    s.active = 0;
     s.and_.nhist = nhist;
     s.and_.iter_euler = iter_euler <= 1 ? 1 : iter_euler;
     s.and_.lam_euler = lam_euler;
   });
 }
 int pf_anderson_setup(pf_system* sys) { return guard(sys, [&](pf::System& s) { s.anderson_setup(); }); }
+
+int pf_euler_create(pf_system* sys, int method, double lam) {
+  return guard(sys, [&](pf::System& s) {
+    if (method != 0 && method != 1)
+      throw pf::PFError(PF_EARG, "Invalid `method` parameter for EulerUpdater. Options include: (:PEC, :PECE)");
+    s.su.reset(1, method, lam);
+    s.active = 1;
+  });
+}
+int pf_momentum_create(pf_system* sys, int method, double lam, double gamma, double beta1, double beta2) {
+  return guard(sys, [&](pf::System& s) {
+    if (method < 0 || method > 3)
+      throw pf::PFError(PF_EARG,
+                        "Invalid `method` parameter for MomentumUpdater. Options include: (:MOM, :RMS, :ADAM, :NAG)");
+    if (!(gamma > 0.0 && gamma < 1.0) || !(beta1 > 0.0 && beta1 < 1.0) || !(beta2 > 0.0 && beta2 < 1.0))
+      throw pf::PFError(PF_EARG, "AssertionError: 0 < gamma, beta1, beta2 < 1");
+    s.su.reset(2, method, lam);
+    s.su.gamma = gamma;
+    s.su.beta1 = beta1;
+    s.su.beta2 = beta2;
+    s.active = 2;
+  });
+}
+int pf_updater_setup(pf_system* sys) { return guard(sys, [&](pf::System& s) { s.updater_setup(); }); }
+int pf_updater_step(pf_system* sys) {
+  return guard(sys, [&](pf::System& s) {
+    s.updater_step();
+    PF_CU(cudaStreamSynchronize(s.st));
+  });
+}
 int pf_anderson_step(pf_system* sys) {
   return guard(sys, [&](pf::System& s) {
     s.anderson_step();

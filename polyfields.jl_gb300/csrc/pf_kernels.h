@@ -152,6 +152,15 @@ void launch_adj_point(double* wbar, const double* rho, const double* rb, const d
 void launch_daxpy(double* y, const double* x, double a, long n, cudaStream_t st);
 // sum_x a_x * b_x into *out (device), float64, deterministic
 void launch_ddot(const double* a, const double* b, long n, double* part, double* out, cudaStream_t st);
+// ---- Euler and momentum field updaters (pf_adjoint.cu), n = nmon * Ng
+void launch_euler_predict(double* w, double* temp, const double* r, double lam, long n, cudaStream_t st);
+void launch_euler_correct(double* w, const double* temp, const double* r, double lam, long n, cudaStream_t st);
+// method 0 MOM, 1 RMS, 2 ADAM
+void launch_momentum(int method, double* w, double* m, double* v, const double* r, double lam, double b1, double b2,
+                     long n, cudaStream_t st);
+void launch_nag_ahead(double* w, double* temp, const double* m, double lam, long n, cudaStream_t st);
+void launch_nag_update(double* w, const double* temp, double* m, const double* r, double lam, double gamma, long n,
+                       cudaStream_t st);
 // Nonzero when a pipelined kernel of this precision gave up waiting on a copy since the
 // last call (reads and clears a device flag; synchronises the stream).
 template <typename T>

@@ -67,6 +67,11 @@ SIGNATURES = {
     "pf_domain_step": (_c_int, [_vp, _c_int]),
     "pf_domain_stress_error": (_c_int, [_vp, _dptr]),
     "pf_scft": (_c_int, [_vp, ctypes.POINTER(ScftOptions), _c_int, ctypes.POINTER(ScftResults)]),
+    "pf_euler_create": (_c_int, [_vp, _c_int, ctypes.c_double]),
+    "pf_momentum_create": (_c_int, [_vp, _c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double]),
+    "pf_updater_setup": (_c_int, [_vp]),
+    "pf_updater_step": (_c_int, [_vp]),
     "pf_set_density_cotangent": (_c_int, [_vp, _c_int, _dptr]),
     "pf_density_pullback": (_c_int, [_vp, _dptr, _c_int, _dptr, _c_int]),
     "pf_scft_batch": (_c_int, [ctypes.POINTER(_vp), _c_int, ctypes.POINTER(ScftOptions), _c_int,

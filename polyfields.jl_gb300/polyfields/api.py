@@ -473,6 +473,63 @@ class AndersonUpdater:
         L.check(L.load().pf_anderson_step(self.system._h), self.system._h)
 
 
+class EulerUpdater:
+    """EulerUpdater(; method = :PECE, lam = 0.05) — euler.jl:9-29 (predictor-corrector Euler)."""
+
+    _METHODS = {"PEC": 0, "PECE": 1}
+
+    def __init__(self, method: str = "PECE", lam: float = 0.05):
+        method = str(method).lstrip(":")
+        if method not in self._METHODS:
+            raise ValueError("Invalid `method` parameter for EulerUpdater. Options include: (:PEC, :PECE)")
+        self.method, self.lam = method, float(lam)
+        self.system: Optional[FieldSystem] = None
+
+    def _bind(self, sys: FieldSystem) -> None:
+        L.check(L.load().pf_euler_create(sys._h, self._METHODS[self.method], self.lam), sys._h)
+        self.system = sys
+
+    def setup(self, sys: FieldSystem) -> None:
+        self._bind(sys)
+        L.check(L.load().pf_updater_setup(sys._h), sys._h)
+
+    def step(self) -> None:
+        if self.system is None:
+            raise RuntimeError("EulerUpdater is not set up")
+        L.check(L.load().pf_updater_step(self.system._h), self.system._h)
+
+
+class MomentumUpdater:
+    """MomentumUpdater(; method = :MOM, lam = 0.01, gamma = 0.9, beta1 = 0.9, beta2 = 0.999)
+    — momentum.jl:19-47 (MOM, RMS, ADAM, NAG)."""
+
+    _METHODS = {"MOM": 0, "RMS": 1, "ADAM": 2, "NAG": 3}
+
+    def __init__(self, method: str = "MOM", lam: float = 0.01, gamma: float = 0.9, beta1: float = 0.9,
+                 beta2: float = 0.999):
+        assert 0.0 < gamma < 1.0 and 0.0 < beta1 < 1.0 and 0.0 < beta2 < 1.0
+        method = str(method).lstrip(":")
+        if method not in self._METHODS:
+            raise ValueError("Invalid `method` parameter for MomentumUpdater. Options include: (:MOM, :RMS, :ADAM, :NAG)")
+        self.method, self.lam = method, float(lam)
+        self.gamma, self.beta1, self.beta2 = float(gamma), float(beta1), float(beta2)
+        self.system: Optional[FieldSystem] = None
+
+    def _bind(self, sys: FieldSystem) -> None:
+        L.check(L.load().pf_momentum_create(sys._h, self._METHODS[self.method], self.lam, self.gamma, self.beta1,
+                                            self.beta2), sys._h)
+        self.system = sys
+
+    def setup(self, sys: FieldSystem) -> None:
+        self._bind(sys)
+        L.check(L.load().pf_updater_setup(sys._h), sys._h)
+
+    def step(self) -> None:
+        if self.system is None:
+            raise RuntimeError("MomentumUpdater is not set up")
+        L.check(L.load().pf_updater_step(self.system._h), self.system._h)
+
+
 class DomainUpdater:
     """DomainUpdater(; nper = 10, nskip = 200, lam = 0.1, pmax = 1.0, rlxn = 0.5) — domain.jl:20-24."""
 
@@ -541,8 +598,8 @@ class SCFTResults:
 def scft(sys: FieldSystem, updater: AndersonUpdater, domain: Optional[DomainUpdater] = None,
          opts: Optional[SCFTOptions] = None) -> SCFTResults:
     """scft!(sys, updater; domain, opts) — src/simulate.jl:60-148."""
-    if not isinstance(updater, AndersonUpdater):
-        raise TypeError("the GPU engine implements scft! with the AndersonUpdater")
+    if not isinstance(updater, (AndersonUpdater, EulerUpdater, MomentumUpdater)):
+        raise TypeError("the GPU engine implements scft! with the Anderson, Euler and Momentum updaters")
     opts = opts or SCFTOptions()
     updater._bind(sys)
     if domain is not None:

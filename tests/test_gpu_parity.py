@@ -267,3 +267,41 @@ def test_density_graph_replay_follows_fields_and_cell(prec, tol):
         assert g.species[0].Q == pytest.approx(o.species[0].Q, rel=tol), k
         for mid in (1, 2):
             assert rel(g.density[mid], o.density[mid]) < tol, (k, mid)
+
+
+UPDATERS = [("euler_PEC", "Euler", dict(method="PEC", lam=0.05)), ("euler_PECE", "Euler", dict(method="PECE", lam=0.05)),
+            ("mom", "Momentum", dict(method="MOM", lam=0.05)), ("rms", "Momentum", dict(method="RMS", lam=0.005)),
+            ("adam", "Momentum", dict(method="ADAM", lam=0.005)), ("nag", "Momentum", dict(method="NAG", lam=0.05))]
+
+
+@pytest.mark.parametrize("case", [CASES[2], CASES[4]], ids=[CASES[2][0], CASES[4][0]])
+@pytest.mark.parametrize("uname,kind,ukw", UPDATERS, ids=[u[0] for u in UPDATERS])
+def test_euler_momentum_steps_fp64(uname, kind, ukw, case):
+    """12 steps of EulerUpdater (euler.jl:37-65, predictor on the updated field as the
+    reference does) and MomentumUpdater (momentum.jl:63-165) against the oracle."""
+    name, kw = case
+    o = SY.diblock_system(O, **kw)
+    g = SY.diblock_system(pf, precision="fp64", **kw)
+    uo = O.EulerUpdater(**ukw) if kind == "Euler" else O.MomentumUpdater(**ukw)
+    ug = pf.EulerUpdater(**ukw) if kind == "Euler" else pf.MomentumUpdater(**ukw)
+    uo.setup(o)
+    ug.setup(g)
+    for _ in range(12):
+        uo.step()
+        ug.step()
+    for mid in (1, 2):
+        assert rel(g.fields[mid], o.fields[mid]) < 1e-9, mid
+
+
+def test_scft_with_euler_updater_fp64():
+    """scft! drives any field updater (simulate.jl:60-148): EulerUpdater(:PECE) on the README
+    lamellar system reaches the oracle's state step for step."""
+    kw = dict(dims=(64, 1, 1), crystal="lamellar", params=(10.0,))
+    o = SY.diblock_system(O, **kw)
+    g = SY.diblock_system(pf, precision="fp64", **kw)
+    ro = O.scft(o, O.EulerUpdater(method="PECE", lam=0.1), opts=O.SCFTOptions(nsteps=60, ftol=1e-12))
+    rg = pf.scft(g, pf.EulerUpdater(method="PECE", lam=0.1), opts=pf.SCFTOptions(nsteps=60, ftol=1e-12))
+    assert rg.nsteps == ro.nsteps
+    assert rg.fhelm == pytest.approx(ro.fhelm, rel=1e-10)
+    for mid in (1, 2):
+        assert rel(g.fields[mid], o.fields[mid]) < 1e-9
