@@ -82,6 +82,10 @@ int pf_system_destroy(pf_system* sys);
 const char* pf_last_error(const pf_system* sys);
 int pf_set_precision(pf_system* sys, int precision);
 int pf_get_precision(const pf_system* sys, int* precision);
+/* FieldSystem(...; mde = :RK2 | :RQM4) (src/system/system.jl:53, src/system/mde.jl:7-41):
+ * 0 = RK2 operator splitting, 1 = RQM4 Richardson extrapolation of one full and two half RK2
+ * steps (mde.jl:83-104; float64 chains only: PF_EUNSUPPORTED with PF_FP32). */
+int pf_set_mde(pf_system* sys, int method);
 
 /* UnitCell(dim, crystal, params) + add_cell!  (src/system/cell.jl:31-52, system.jl:102-106).
  * crystal is the reference's Symbol name without ':' ("lamellar", "hexagonal", "cubic", ...). */

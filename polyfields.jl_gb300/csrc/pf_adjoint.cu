@@ -241,3 +241,21 @@ void launch_nag_update(double* w, const double* temp, double* m, const double* r
 }
 
 }  // namespace pf
+
+// ------------------------------------------------------------------ RQM4 combination
+// src/system/mde.jl:83-104: q_{s+1} = (4 q2 - q1) / 3 with q1 one full RK2 step and q2 two
+// half steps from q_s.
+namespace pf {
+template <typename T>
+__global__ void rqm4_combine_kernel(T* __restrict__ out, const T* __restrict__ q1, const T* __restrict__ q2, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    out[i] = (T)((4.0 * (double)q2[i] - (double)q1[i]) / 3.0);
+}
+template <typename T>
+void launch_rqm4_combine(T* out, const T* q1, const T* q2, long n, cudaStream_t st) {
+  rqm4_combine_kernel<T><<<adj_blocks(n), 256, 0, st>>>(out, q1, q2, n);
+  count_launches(1);
+}
+template void launch_rqm4_combine<float>(float*, const float*, const float*, long, cudaStream_t);
+template void launch_rqm4_combine<double>(double*, const double*, const double*, long, cudaStream_t);
+}  // namespace pf

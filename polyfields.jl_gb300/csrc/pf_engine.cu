@@ -336,6 +336,11 @@ struct Species {
   // forward and backward jobs, the Simpson factors fac[s] and the mean of the last q
   DevBuf csc[2], lsc[2], fac, meanq;
   int ld_version[2] = {-1, -1};
+  // RQM4 (float64): half-step operators per block, one-step and two-half-step jobs per block
+  std::vector<std::unique_ptr<DevBuf>> lw2, ld2;
+  DevBuf rq_ops, rq_jobs;
+  std::vector<const double*> rq_ld1, rq_ld2;  // host: LD of the full and the half steps
+  int ld2_version = -1;
   DevBuf Qdev;
   bool Q_valid = false;
   int nblocks() const { return (int)N_block.size(); }
@@ -420,6 +425,8 @@ struct System {
   }
   bool jobs_dirty[2] = {true, true};
   bool timing = false;
+  int mde = 0;     // 0 RK2 (mde.jl:65-81), 1 RQM4 (mde.jl:83-104, float64 chains)
+  DevBuf rq_scratch;  // RQM4: [x, q1] and [x, h, q2]
   // density solves replay a captured CUDA graph per precision (PF_NO_GRAPHS=1 disables)
   bool use_graphs = true;
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
@@ -778,6 +785,94 @@ struct System {
     jobs_dirty[p] = false;
   }
 
+  // ---------------------------------------------------------------- RQM4 chains (float64)
+  void ensure_rqm4() {
+    rq_scratch.alloc(sizeof(double) * 5 * ng);
+    for (auto& spp : species) {
+      Species& sp = *spp;
+      if (sp.kind != 0) continue;
+      const int nb = sp.nblocks();
+      if ((int)sp.lw2.size() != nb) {
+        sp.lw2.clear();
+        sp.ld2.clear();
+        for (int b = 0; b < nb; ++b) {
+          sp.lw2.emplace_back(new DevBuf());
+          sp.lw2.back()->alloc(sizeof(double) * ng);
+          sp.ld2.emplace_back(new DevBuf());
+          sp.ld2.back()->alloc(sizeof(double) * nk);
+        }
+        sp.ld2_version = -1;
+      }
+      // per block: ops {LW, LD} then 2 x {LW2, LD2}; jobs: one full step on [x, q1], two half
+      // steps on [x, h, q2]
+      std::vector<StepOp<double>> hops;
+      std::vector<ChainJob<double>> hj;
+      double* X = rq_scratch.as<double>();
+      double* Y = X + 2 * ng;
+      Cx<double>* kb = nz > 1 ? sp.kbuf[0][0].as<Cx<double>>() : nullptr;
+      sp.rq_ld1.clear();
+      sp.rq_ld2.clear();
+      for (int b = 0; b < nb; ++b) {
+        hops.push_back(StepOp<double>{sp.lw[0][b]->as<double>(), sp.ld[0][b]->as<double>()});
+        hops.push_back(StepOp<double>{sp.lw2[b]->as<double>(), sp.ld2[b]->as<double>()});
+        hops.push_back(StepOp<double>{sp.lw2[b]->as<double>(), sp.ld2[b]->as<double>()});
+        sp.rq_ld1.push_back(sp.ld[0][b]->as<double>());
+        sp.rq_ld2.push_back(sp.ld2[b]->as<double>());
+      }
+      sp.rq_ops.alloc(sizeof(StepOp<double>) * hops.size());
+      PF_CU(cudaMemcpy(sp.rq_ops.p, hops.data(), sp.rq_ops.bytes, cudaMemcpyHostToDevice));
+      const StepOp<double>* ops = sp.rq_ops.as<StepOp<double>>();
+      for (int b = 0; b < nb; ++b) {
+        hj.push_back(ChainJob<double>{X, ops + 3 * b, kb, nullptr, nullptr, 0, +1, 1, 0});
+        hj.push_back(ChainJob<double>{Y, ops + 3 * b + 1, kb, nullptr, nullptr, 0, +1, 2, 0});
+      }
+      sp.rq_jobs.alloc(sizeof(ChainJob<double>) * hj.size());
+      PF_CU(cudaMemcpy(sp.rq_jobs.p, hj.data(), sp.rq_jobs.bytes, cudaMemcpyHostToDevice));
+    }
+  }
+  // x -> y by one RQM4 step of block b: y = (4 q2 - q1) / 3
+  void rqm4_step(Species& sp, int b, const double* x, double* y) {
+    double* X = rq_scratch.as<double>();
+    double* Y = X + 2 * ng;
+    PF_CU(cudaMemcpyAsync(X, x, sizeof(double) * ng, cudaMemcpyDeviceToDevice, st));
+    PF_CU(cudaMemcpyAsync(Y, x, sizeof(double) * ng, cudaMemcpyDeviceToDevice, st));
+    const ChainJob<double>* jd = sp.rq_jobs.as<ChainJob<double>>() + 2 * b;
+    const GridDims dims{nx, ny, nz};
+    const double* ld1[1] = {sp.rq_ld1[b]};
+    const double* ld2[2] = {sp.rq_ld2[b], sp.rq_ld2[b]};
+    ChainHost<double> h1, h2;
+    h1.kbuf = h2.kbuf = nz > 1 ? sp.kbuf[0][0].as<Cx<double>>() : nullptr;
+    h1.nsteps = 1;
+    h1.ld = ld1;
+    h2.nsteps = 2;
+    h2.ld = ld2;
+    launch_chains<double>(jd, 1, 1, dims, tw<double>(0), st, &h1);
+    launch_chains<double>(jd + 1, 1, 2, dims, tw<double>(0), st, &h2);
+    launch_rqm4_combine<double>(y, X + ng, Y + 2 * ng, ng, st);
+    check_launch();
+  }
+  void rqm4_chains() {
+    for (auto& spp : species) {
+      Species& sp = *spp;
+      if (sp.kind != 0) continue;
+      const int nb = sp.nblocks(), Ns = sp.Ns;
+      double* q = sp.q[0].as<double>();
+      for (int t = 0; t < Ns; ++t) {
+        int b = 0;
+        while (!(sp.begin_block[b] - 1 <= t && t < sp.begin_block[b + 1] - 1)) ++b;
+        rqm4_step(sp, b, q + (long)t * ng, q + (long)(t + 1) * ng);
+      }
+      if (nb > 1) {
+        double* qc = sp.qc[0].as<double>();
+        for (int s = Ns; s >= 1; --s) {
+          int b = 0;
+          while (!(sp.begin_block[b] - 1 < s && s <= sp.begin_block[b + 1] - 1)) ++b;
+          rqm4_step(sp, b, qc + (long)s * ng, qc + (long)(s - 1) * ng);
+        }
+      }
+    }
+  }
+
   // ---------------------------------------------------------------- density solve body
   bool capturing = false;
   void record_ev(int i) {
@@ -797,12 +892,16 @@ struct System {
       for (int b = 0; b < sp.nblocks(); ++b) {
         const auto& m = monomers.at(sp.mid_block[b]);
         launch_lw<T>(sp.lw[p][b]->as<T>(), grid_ptr(w, sp.mid_block[b]), sp.ds_block[b] / 2.0 * m.first, ng, st);
+        if (mde == 1)  // half-step factor exp(-ds vol w / 4)
+          launch_lw<double>(sp.lw2[b]->as<double>(), grid_ptr(w, sp.mid_block[b]), sp.ds_block[b] / 4.0 * m.first,
+                            ng, st);
       }
       launch_fill<T>(sp.q[p].as<T>(), (T)1, ng, st);
       if (sp.nblocks() > 1) launch_fill<T>(sp.qc[p].as<T>() + (long)sp.Ns * ng, (T)1, ng, st);
     }
     record_ev(1);
-    if (njobs)
+    if (mde == 1) rqm4_chains();
+    else if (njobs)
       launch_chains<T>(jobs[p].as<ChainJob<T>>(), njobs, maxsteps, GridDims{nx, ny, nz}, tw<T>(p), st,
                        hosts_of<T>().data(), branches());
     record_ev(2);
@@ -846,6 +945,10 @@ struct System {
   void density_t(int p) {
     require_ready();
     ensure_prop<T>(p);
+    if (mde == 1) {
+      if (p != 0) throw PFError(E_UNSUPPORTED, "the RQM4 propagator runs with float64 chains");
+      ensure_rqm4();
+    }
     // bond operators: regenerated (outside the graph) when the cell changed
     const CellGeom g = geom();
     mde_steps = 0;
@@ -857,10 +960,16 @@ struct System {
           launch_ld<T>(sp.ld[p][b]->as<T>(), g, sp.ds_block[b] * sp.b_block[b] * sp.b_block[b] / 6.0,
                        1.0 / (double)ng, nk, st);
       sp.ld_version[p] = cell_version;
+      if (mde == 1 && sp.ld2_version != cell_version) {
+        for (int b = 0; b < sp.nblocks(); ++b)
+          launch_ld<double>(sp.ld2[b]->as<double>(), g, sp.ds_block[b] * sp.b_block[b] * sp.b_block[b] / 12.0,
+                            1.0 / (double)ng, nk, st);
+        sp.ld2_version = cell_version;
+      }
       mde_steps += sp.Ns * (sp.nblocks() > 1 ? 2 : 1);
     }
     check_launch();
-    if (!use_graphs) {
+    if (!use_graphs || mde == 1) {
       density_enqueue<T>(p);
     } else if (gexec[p]) {
       PF_CU(cudaGraphLaunch(gexec[p], st));
@@ -1340,6 +1449,7 @@ struct System {
   template <typename T>
   void pullback_t(int p, std::vector<double>& cell_bar, std::vector<double>& nref_bar) {
     require_ready();
+    if (mde != 0) throw PFError(E_UNSUPPORTED, "the pullback differentiates the RK2 propagator");
     density_t<T>(p);
     fetch_Q();
     const int npr = cell.np(), nw = npr + 1;
@@ -1712,6 +1822,15 @@ int pf_set_precision(pf_system* sys, int precision) {
   return guard(sys, [&](pf::System& s) {
     if (precision != PF_FP64 && precision != PF_FP32) throw pf::PFError(PF_EARG, "precision must be PF_FP64 or PF_FP32");
     s.prec = precision;
+  });
+}
+
+int pf_set_mde(pf_system* sys, int method) {
+  return guard(sys, [&](pf::System& s) {
+    if (method != 0 && method != 1)
+      throw pf::PFError(PF_EARG, "Invalid propagator method for PseudoSpectralSolver: 0 = :RK2, 1 = :RQM4");
+    s.mde = method;
+    s.invalidate_graphs();
   });
 }
 

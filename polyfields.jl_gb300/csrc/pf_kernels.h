@@ -161,6 +161,9 @@ void launch_momentum(int method, double* w, double* m, double* v, const double* 
 void launch_nag_ahead(double* w, double* temp, const double* m, double lam, long n, cudaStream_t st);
 void launch_nag_update(double* w, const double* temp, double* m, const double* r, double lam, double gamma, long n,
                        cudaStream_t st);
+// RQM4: out = (4 q2 - q1) / 3 (pf_adjoint.cu)
+template <typename T>
+void launch_rqm4_combine(T* out, const T* q1, const T* q2, long n, cudaStream_t st);
 // Nonzero when a pipelined kernel of this precision gave up waiting on a copy since the
 // last call (reads and clears a device flag; synchronises the stream).
 template <typename T>

@@ -231,8 +231,9 @@ class FieldSystem:
                  precision: str = FP64, mde: str = "RK2"):
         if ensemble != Canonical:
             raise ValueError("the GPU engine implements the canonical ensemble")
-        if mde != "RK2":
-            raise ValueError("the GPU engine implements the :RK2 propagator")
+        mde = str(mde).lstrip(":")
+        if mde not in ("RK2", "RQM4"):
+            raise ValueError(f"Invalid propagator method `{mde}` for PseudoSpectralSolver.")
         dims = tuple(int(d) for d in dims)
         if tuple(sorted(dims, reverse=True)) != dims:
             raise AssertionError("dims must be given in descending order (src/system/system.jl:58)")
@@ -242,6 +243,9 @@ class FieldSystem:
         if st != L.PF_OK:
             raise L.PolyFieldsError(st, f"pf_system_create{dims}: {lib.pf_status_string(st).decode()}")
         self._h = h
+        if mde == "RQM4":
+            L.check(lib.pf_set_mde(h, 1), h)
+        self.mde = mde
         self.dims = dims
         self.shape = (dims[2], dims[1], dims[0])
         self.ensemble = ensemble

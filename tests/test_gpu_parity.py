@@ -305,3 +305,29 @@ def test_scft_with_euler_updater_fp64():
     assert rg.fhelm == pytest.approx(ro.fhelm, rel=1e-10)
     for mid in (1, 2):
         assert rel(g.fields[mid], o.fields[mid]) < 1e-9
+
+
+@pytest.mark.parametrize("name,kw", [CASES[0], CASES[2], CASES[4]], ids=[CASES[0][0], CASES[2][0], CASES[4][0]])
+def test_rqm4_density_fp64(name, kw):
+    """FieldSystem(...; mde = :RQM4): Richardson extrapolation (4 q2 - q1) / 3 of one full and two
+    half RK2 steps per contour step (mde.jl:83-104), float64 chains: Q, densities, free energy
+    and stress against the oracle's RQM4 solver."""
+    def build(M, **extra):
+        A, B = M.Monomer(1, 1.0), M.Monomer(2, 1.0)
+        dims = kw["dims"]
+        nd = sum(1 for d in dims if d > 1)
+        s = M.FieldSystem(dims, M.UnitCell(nd, kw["crystal"], *kw["params"]), monomers=[A, B], mde="RQM4", **extra)
+        s.add_species(M.Diblock(A, B, 100, kw.get("f", 0.5), 1.0, 1.0, 100), 1.0)
+        itx = M.FloryInteraction()
+        itx.set_interaction(A, B, kw.get("chi", 0.2))
+        s.add_interaction(itx)
+        shape = (dims[2], dims[1], dims[0])
+        M.fieldinit(s, SY.seeded_fields(shape, [1, 2], 31, 0.3))
+        return s
+    o = build(O)
+    g = build(pf, precision="fp64")
+    assert g.species[0].Q == pytest.approx(o.species[0].Q, rel=FP64_RTOL)
+    for mid in (1, 2):
+        assert rel(g.density[mid], o.density[mid]) < FP64_RTOL
+    assert g.free_energy() == pytest.approx(o.free_energy(), rel=FP64_RTOL)
+    assert np.allclose(g.scfstress(), o.scfstress(), rtol=1e-9, atol=1e-14)
