@@ -136,8 +136,8 @@ def bcc_system(M, n=64, L=7.0, precision=None, Ns=100, seed=12345):
     """The 3D BCC workload: AB diblock N100 fA0.30 (built as Multiblock([A, B], [30, 70])),
     chi 0.2, Ns 100, cubic cell L0; w_A = 0.1 N(0,1) + the sum of cos(2 pi h.r / L) over the 12
     {110} reflections (h = (+-1, +-1, 0) and permutations; fractional coordinates on the
-    grid) scaled to amplitude 1.0 (the raw sum peaks at 12, which as a field would overflow
-    the propagators), w_B = -w_A."""
+    grid) scaled by 1/4 (peak 3; the raw sum peaks at 12, which as a field overflows float64
+    propagators at ds = 1, and a peak of 1 decays to the disordered state), w_B = -w_A."""
     A, B = M.Monomer(1), M.Monomer(2)
     sys = _fs(M, (n, n, n), M.UnitCell(3, "cubic", L), [A, B], precision)
     sys.add_species(M.Multiblock([A, B], [30, 70], [1.0, 1.0], Ns), 1.0)
@@ -150,6 +150,6 @@ def bcc_system(M, n=64, L=7.0, precision=None, Ns=100, seed=12345):
     for a, b in ((x, y), (y, z), (z, x)):  # 6 +-pairs x 2 signs = 12 reflections
         pat += 2.0 * np.cos(2 * np.pi * (a + b)) + 2.0 * np.cos(2 * np.pi * (a - b))
     rng = np.random.Generator(np.random.PCG64(seed))
-    wa = 0.1 * rng.standard_normal(shape) + pat / 12.0
+    wa = 0.1 * rng.standard_normal(shape) + pat / 4.0
     M.fieldinit(sys, {1: wa, 2: -wa})
     return sys
