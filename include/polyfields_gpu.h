@@ -174,6 +174,11 @@ int pf_scft(pf_system* sys, const pf_scft_options* opts, int use_domain, pf_scft
  * dL/dchi is zero (chi does not enter density! at fixed fields).  Works in the handle's
  * precision; float32 chains keep the forward solve's per-step rescaling. */
 int pf_set_density_cotangent(pf_system* sys, int mid, const double* rho_bar);
+/* every > 0: the pullback reads each chain's propagators only at the checkpoints s = 0,
+ * every, 2 every, ... and recomputes the contour steps in between (one segment at a time,
+ * into a buffer of every + 1 grids) instead of reading every stored step; 0 (the default):
+ * read the stored histories. */
+int pf_set_adjoint_checkpoints(pf_system* sys, int every);
 int pf_density_pullback(pf_system* sys, double* cell_bar, int ncell, double* nref_bar, int nnref);
 
 /* Many independent scft! runs (a phase-diagram sweep: src/simulate.jl:60-148 once per

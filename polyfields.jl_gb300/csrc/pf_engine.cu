@@ -426,6 +426,7 @@ struct System {
   bool jobs_dirty[2] = {true, true};
   bool timing = false;
   int mde = 0;     // 0 RK2 (mde.jl:65-81), 1 RQM4 (mde.jl:83-104, float64 chains)
+  int adj_ckpt = 0;  // pullback: 0 = read the stored histories, K > 0 = recompute between checkpoints
   DevBuf rq_scratch;  // RQM4: [x, q1] and [x, h, q2]
   // density solves replay a captured CUDA graph per precision (PF_NO_GRAPHS=1 disables)
   bool use_graphs = true;
@@ -1487,6 +1488,16 @@ struct System {
     const T* const* src_dev = reinterpret_cast<const T* const*>(ptrs.as<void*>());
     Cx<T>* const* dst_dev = reinterpret_cast<Cx<T>* const*>(ptrs.as<void*>() + 2);
     const double* rb = rbar.as<double>();
+    // checkpointed walks: each chain's propagators are recomputed segment by segment (K steps
+    // from the stored checkpoint q_{cK}) into a (K+1)-grid buffer, with scratch rescale factors
+    const int K = adj_ckpt;
+    DevBuf segb, segcsc, seglsc, segjobs;
+    if (K > 0) {
+      segb.alloc(sizeof(T) * (size_t)(K + 1) * ng);
+      segcsc.alloc(sizeof(float) * K);
+      seglsc.alloc(sizeof(double) * K);
+    }
+    int jobidx = 0;  // index of the species' forward job in the host views
     auto dot_host = [&](const double* a, const double* b) {
       launch_ddot(a, b, ng, dpart.as<double>(), dots.as<double>(), st);
       double v = 0.0;
@@ -1581,23 +1592,72 @@ struct System {
         launch_adj_finish<T>(lam, rr, lam, x, y, G.as<double>() + (size_t)b * ng, cfac, src, ng, st);
         check_launch();
       };
+      // segment jobs: chain 0 (forward, ops[t]) and chain 1 (backward, ops[Ns + t'])
+      const int nseg = K > 0 ? (Ns + K - 1) / K : 0;
+      if (K > 0) {
+        std::vector<ChainJob<T>> sj;
+        for (int ch = 0; ch < 2; ++ch)
+          for (int c = 0; c < nseg; ++c)
+            sj.push_back(ChainJob<T>{segb.as<T>(), ops + (ch ? Ns : 0) + c * K, nz > 1 ? k1 : nullptr,
+                                     scaled(p) ? segcsc.as<float>() : nullptr,
+                                     scaled(p) ? seglsc.as<double>() : nullptr, 0, +1, std::min(K, Ns - c * K), 0});
+        segjobs.alloc(sizeof(ChainJob<T>) * sj.size());
+        PF_CU(cudaMemcpy(segjobs.p, sj.data(), segjobs.bytes, cudaMemcpyHostToDevice));
+      }
+      // propagators of segment c of chain ch: B[j] = step c*K + j of that chain, from its checkpoint
+      auto recompute = [&](int ch, int c, const T* start) {
+        T* B = segb.as<T>();
+        PF_CU(cudaMemcpyAsync(B, start, sizeof(T) * ng, cudaMemcpyDeviceToDevice, st));
+        ChainHost<T> h;
+        h.kbuf = nz > 1 ? k1 : nullptr;
+        h.csc = scaled(p) ? segcsc.as<float>() : nullptr;
+        h.lsc = scaled(p) ? seglsc.as<double>() : nullptr;
+        h.nsteps = std::min(K, Ns - c * K);
+        h.ld = lds_of<T>()[jobidx + ch].data() + c * K;
+        launch_chains<T>(segjobs.as<ChainJob<T>>() + ch * nseg + c, 1, h.nsteps, dims, tw<T>(p), st, &h);
+        check_launch();
+        return static_cast<const T*>(B);
+      };
       // forward chain q_{t+1} = A q_t: adjoint from t = Ns down to 0
       launch_adj_init<T>(lam, src_at(Ns, true), dq, ng, st);
+      int cur = -1;
+      const T* B = nullptr;
       for (int t = Ns - 1; t >= 0; --t) {
         int b = 0;
         while (!(b0(b) <= t && t < b1(b))) ++b;
         const float* cf = scaled(p) ? sp.csc[0].as<float>() + t : nullptr;
-        step(t, b, q + (long)t * ng, q + (long)(t + 1) * ng, cf, src_at(t, true));
+        const T* x = q + (long)t * ng;
+        if (K > 0) {
+          const int c = t / K;
+          if (c != cur) {
+            B = recompute(0, c, q + (long)c * K * ng);
+            cur = c;
+          }
+          x = B + (long)(t - c * K) * ng;
+        }
+        step(t, b, x, x + ng, cf, src_at(t, true));
       }
       if (!homo) {
         // backward chain qc_{s-1} = A qc_s: adjoint from s = 0 up to Ns
         launch_adj_init<T>(lam, src_at(0, false), 0.0, ng, st);
+        cur = -1;
         for (int s = 1; s <= Ns; ++s) {
           int b = 0;
           while (!(b0(b) < s && s <= b1(b))) ++b;
           const int tp = Ns - s;
           const float* cf = scaled(p) ? sp.csc[1].as<float>() + tp : nullptr;
-          step(Ns + tp, b, qc + (long)s * ng, qc + (long)(s - 1) * ng, cf, src_at(s, false));
+          const T* x = qc + (long)s * ng;
+          const T* y = qc + (long)(s - 1) * ng;
+          if (K > 0) {
+            const int c = tp / K;
+            if (c != cur) {
+              B = recompute(1, c, qc + (long)(Ns - c * K) * ng);
+              cur = c;
+            }
+            x = B + (long)(tp - c * K) * ng;
+            y = x + ng;
+          }
+          step(Ns + tp, b, x, y, cf, src_at(s, false));
         }
       }
       // w gradients and the ds / Nref terms of every block
@@ -1613,6 +1673,7 @@ struct System {
         const double dds = hacc[(size_t)b * nw + npr] - vol / 2.0 * wg + contrib[b] / sp.ds_block[b];
         nref_bar.push_back(dds / (double)(b1(b) - b0(b)) - S / sp.Nref);
       }
+      jobidx += homo ? 1 : 2;
     }
     PF_CU(cudaStreamSynchronize(st));
     check_pipe(p);
@@ -1822,6 +1883,13 @@ int pf_set_precision(pf_system* sys, int precision) {
   return guard(sys, [&](pf::System& s) {
     if (precision != PF_FP64 && precision != PF_FP32) throw pf::PFError(PF_EARG, "precision must be PF_FP64 or PF_FP32");
     s.prec = precision;
+  });
+}
+
+int pf_set_adjoint_checkpoints(pf_system* sys, int every) {
+  return guard(sys, [&](pf::System& s) {
+    if (every < 0) throw pf::PFError(PF_EARG, "checkpoint interval must be >= 0");
+    s.adj_ckpt = every;
   });
 }
 

@@ -74,6 +74,7 @@ SIGNATURES = {
     "pf_updater_setup": (_c_int, [_vp]),
     "pf_updater_step": (_c_int, [_vp]),
     "pf_set_density_cotangent": (_c_int, [_vp, _c_int, _dptr]),
+    "pf_set_adjoint_checkpoints": (_c_int, [_vp, _c_int]),
     "pf_density_pullback": (_c_int, [_vp, _dptr, _c_int, _dptr, _c_int]),
     "pf_scft_batch": (_c_int, [ctypes.POINTER(_vp), _c_int, ctypes.POINTER(ScftOptions), _c_int,
                                ctypes.POINTER(ScftResults), ctypes.POINTER(_c_int), _c_int]),

@@ -363,6 +363,11 @@ class FieldSystem:
         L.check(L.load().pf_get_propagator(self._h, isp, 1 if conjugate else 0, s, L.dptr(out)), self._h)
         return out
 
+    def set_adjoint_checkpoints(self, every: int) -> None:
+        """Pullback reads the propagators only every ``every`` contour steps and recomputes the
+        steps in between (0: read all stored steps)."""
+        L.check(L.load().pf_set_adjoint_checkpoints(self._h, int(every)), self._h)
+
     def density_pullback(self, rho_bar: Dict[int, np.ndarray]) -> Dict:
         """Pullback of density!(sys) for a loss L with dL/drho_m = rho_bar[m] (monomers not
         listed: zero).  Recomputes the density at the current fields and cell, then returns

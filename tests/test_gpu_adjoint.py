@@ -115,8 +115,9 @@ def test_torch_autograd_density_matches_pullback():
 
 def test_adjoint_96cubed_against_reference_gradient_and_differences():
     """The differentiation workload: 96^3 cubic cell L = 8, AB diblock N = 100, fA = 0.35,
-    Ns = 200, chi = 0.2; L = sum (rho_A - target)^2 with a smooth seeded target (5 lowest
-    modes, amplitude 0.2, mean fA).  GPU FP64 vs the FP64 CPU reference gradient (1e-9),
+    Ns = 200, chi = 0.2, propagators recomputed between checkpoints every 15 contour steps;
+    L = sum (rho_A - target)^2 with a smooth seeded target (5 lowest modes, amplitude 0.2,
+    mean fA).  GPU FP64 vs the FP64 CPU reference gradient (1e-9),
     GPU FP32 chains vs the same (1e-3), and central differences with h = 1e-4 for w_A, w_B,
     L (GPU FP64 losses), fA (reference continuous relaxation) and chi (zero)."""
     dims, shape = (96, 96, 96), (96, 96, 96)
@@ -141,8 +142,12 @@ def test_adjoint_96cubed_against_reference_gradient_and_differences():
     o.density_update()
     _, rbar = AD.density_loss(o, 1, target)
     go = AD.density_pullback(o, rbar)
-    g64 = make(pf, "fp64").density_pullback(rbar)
-    g32 = make(pf, "fp32").density_pullback(rbar)
+    s64, s32 = make(pf, "fp64"), make(pf, "fp32")
+    s64.set_adjoint_checkpoints(15)  # q checkpointed every 15 contour steps
+    s32.set_adjoint_checkpoints(15)
+    g64 = s64.density_pullback(rbar)
+    g32 = s32.density_pullback(rbar)
+    del s64, s32
     for m in (1, 2):
         assert relmax(g64["w"][m], go["w"][m]) < 1e-9
         assert relmax(g32["w"][m], go["w"][m]) < 1e-3
@@ -183,3 +188,23 @@ def test_adjoint_96cubed_against_reference_gradient_and_differences():
 
     fdf = (oracle_loss(35.0 + 100 * h) - oracle_loss(35.0 - 100 * h)) / (2 * h)
     assert dfa64 == pytest.approx(fdf, rel=1e-5)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("name,dims,crystal,params,blend", [CASES[2], CASES[4]], ids=[CASES[2][0], CASES[4][0]])
+def test_checkpointed_pullback_equals_stored(name, dims, crystal, params, blend, prec):
+    """Recomputing the propagators between checkpoints every 15 contour steps gives the same
+    gradients as reading the stored histories (the recompute repeats the forward arithmetic)."""
+    shape = (dims[2], dims[1], dims[0])
+    rng = np.random.default_rng(33)
+    mids = [1, 2, 3] if blend else [1, 2]
+    fields = {m: 0.4 * rng.standard_normal(shape) for m in mids}
+    rbar = {1: rng.standard_normal(shape), 2: rng.standard_normal(shape)}
+    g = build(pf, dims, crystal, params, fields, blend, precision=prec)
+    ref = g.density_pullback(rbar)
+    g.set_adjoint_checkpoints(15)
+    ck = g.density_pullback(rbar)
+    tol = 1e-12 if prec == "fp64" else 1e-6
+    for m in mids:
+        assert relmax(ck["w"][m], ref["w"][m]) < tol, m
+    assert relmax(ck["cell"], ref["cell"]) < tol
