@@ -105,6 +105,14 @@ int pf_add_multiblock(pf_system* sys, int nblocks, const int* block_mids, const 
 int pf_add_point(pf_system* sys, int mid, double phi);
 /* FloryInteraction set_interaction! + add_interaction! (src/interactions/flory.jl:36-49) */
 int pf_set_flory(pf_system* sys, int mid_a, int mid_b, double chi);
+/* set_interaction!(::EdwardsInteraction, mid, u) (src/interactions/edwards.jl:26-33): excluded
+ * volume (u/2) sum (rho_mid / v)^2, potential u rho_mid / v (edwards.jl:34-87). */
+int pf_set_edwards(pf_system* sys, int mid, double u);
+/* FieldSystem(...; ensemble = Canonical | Grand) (src/system/system.jl:6-13, 51-76): 0 =
+ * Canonical (add_species! values are volume fractions), 1 = Grand (they are chemical
+ * potentials mu; phi = Q exp(mu) after each density solve, no mean subtraction).  Must be set
+ * before species are added. */
+int pf_set_ensemble(pf_system* sys, int ensemble);
 
 /* chain_grid(N_block .* vol, Ns) of a species: Ns after adjustment, Nref, begin_block (nblocks+1,
  * 1-based as in the reference) and ds_block (src/species/base.jl:27-56). */

@@ -322,6 +322,7 @@ static bool lu_inverse(std::vector<double> a, int n, std::vector<double>& inv) {
 struct Species {
   int kind = 0;  // 0 multiblock, 1 point
   double phi = 0.0, mu = 0.0, Q = 0.0, Nref = 0.0;
+  double mu_in = 0.0;  // grand ensemble: the chemical potential given to add_species!
   std::vector<int> mids;  // sorted monomer ids
   // multiblock (src/species/multiblock.jl:5-60)
   int Ns = 0, N = 0;
@@ -394,6 +395,7 @@ struct System {
   std::map<int, std::pair<double, double>> monomers;  // id -> (vol, charge)
   std::vector<int> mon_ids;                            // sorted ids; index = position
   std::map<std::pair<int, int>, double> chis;          // ordered pair -> chi
+  std::map<int, double> edwards;                       // monomer id -> u (EdwardsInteraction)
   std::vector<std::unique_ptr<Species>> species;
 
   DevBuf w, pot, res, rho;   // nmon * ng doubles
@@ -427,6 +429,8 @@ struct System {
   bool timing = false;
   int mde = 0;     // 0 RK2 (mde.jl:65-81), 1 RQM4 (mde.jl:83-104, float64 chains)
   int adj_ckpt = 0;  // pullback: 0 = read the stored histories, K > 0 = recompute between checkpoints
+  int ensemble = 0;  // 0 Canonical, 1 Grand (system.jl:6-13)
+  DevBuf one;        // a device 1.0 (grand-canonical densities are not divided by Q)
   DevBuf rq_scratch;  // RQM4: [x, q1] and [x, h, q2]
   // density solves replay a captured CUDA graph per precision (PF_NO_GRAPHS=1 disables)
   bool use_graphs = true;
@@ -494,6 +498,11 @@ struct System {
     packed.alloc(sizeof(double) * 4096);
     cn.alloc(sizeof(double) * kMaxHist);
     status.alloc(sizeof(int) * 4);
+    {
+      const double v1 = 1.0;
+      one.alloc(sizeof(double));
+      PF_CU(cudaMemcpy(one.p, &v1, sizeof(double), cudaMemcpyHostToDevice));
+    }
     build_twiddles<double>(0);
     build_twiddles<float>(1);
     for (auto& e : ev) PF_CU(cudaEventCreate(&e));
@@ -581,6 +590,9 @@ struct System {
       ms.chi[a * kMaxMon + b] = kv.second;
       ms.chi[b * kMaxMon + a] = kv.second;
     }
+    // Edwards excluded volume (edwards.jl:66-87) as the diagonal: pot_a += u_a rho_a / v_a,
+    // energy (u_a / 2) (rho_a / v_a)^2
+    for (auto& kv : edwards) ms.chi[mon_index(kv.first) * kMaxMon + mon_index(kv.first)] = kv.second;
     return ms;
   }
 
@@ -636,8 +648,9 @@ struct System {
     chain_grid(sp->Nref_block, Ns, sp->Nref, sp->begin_block, sp->ds_block);
     for (double v : sp->Nref_block) sp->f_block.push_back(v / sp->Nref);
     sp->Ns = sp->begin_block.back() - 1;  // multiblock.jl:56-59
-    if (phi <= 0.0) throw PFError(E_ARG, "Bulk volume fraction must be 0 < phi <= 1.");
-    sp->phi = phi;
+    if (ensemble == 0 && phi <= 0.0) throw PFError(E_ARG, "Bulk volume fraction must be 0 < phi <= 1.");
+    sp->phi = ensemble == 0 ? phi : 0.0;  // system.jl:148-157
+    sp->mu_in = ensemble == 0 ? 0.0 : phi;
     sp->Qdev.alloc(sizeof(double));
     species.push_back(std::move(sp));
     jobs_dirty[0] = jobs_dirty[1] = true;
@@ -647,12 +660,13 @@ struct System {
   void add_point(int mid, double phi) {
     if (!monomers.count(mid))
       throw PFError(E_ARG, "Species contains monomer with id = " + std::to_string(mid) + " not present in system.");
-    if (phi <= 0.0) throw PFError(E_ARG, "Bulk volume fraction must be 0 < phi <= 1.");
+    if (ensemble == 0 && phi <= 0.0) throw PFError(E_ARG, "Bulk volume fraction must be 0 < phi <= 1.");
     auto sp = std::make_unique<Species>();
     sp->kind = 1;
     sp->mids = {mid};
     sp->Nref = monomers[mid].first;
-    sp->phi = phi;
+    sp->phi = ensemble == 0 ? phi : 0.0;
+    sp->mu_in = ensemble == 0 ? 0.0 : phi;
     sp->Qdev.alloc(sizeof(double));
     species.push_back(std::move(sp));
     invalidate_graphs();
@@ -663,6 +677,11 @@ struct System {
     if (!monomers.count(a) || !monomers.count(b))
       throw PFError(E_ARG, "Interaction contains monomer not present in system.");
     chis[{std::min(a, b), std::max(a, b)}] = chi;
+  }
+
+  void set_edwards(int mid, double u) {  // set_interaction!(::EdwardsInteraction, mid, u)
+    if (!monomers.count(mid)) throw PFError(E_ARG, "Interaction contains monomer not present in system.");
+    edwards[mid] = u;
   }
 
   void set_cell(int dim, const std::string& crystal, const std::vector<double>& params) {
@@ -910,11 +929,12 @@ struct System {
       Species& sp = *spp;
       if (sp.kind == 0) {
         const double* fac = nullptr;
+        const bool grand = ensemble == 1;
         if (scaled(p)) {
           launch_sum<T>(sp.q[p].as<T>() + (long)sp.Ns * ng, ng, part.as<double>(), sp.meanq.as<double>(), (double)ng,
                         st);
           launch_scale_finalize(sp.lsc[0].as<double>(), sp.lsc[1].as<double>(), sp.nblocks() == 1, sp.Ns,
-                                sp.meanq.as<double>(), sp.Qdev.as<double>(), sp.fac.as<double>(), st);
+                                sp.meanq.as<double>(), sp.Qdev.as<double>(), sp.fac.as<double>(), st, !grand);
           fac = sp.fac.as<double>();
         } else {
           launch_sum<T>(sp.q[p].as<T>() + (long)sp.Ns * ng, ng, part.as<double>(), sp.Qdev.as<double>(), (double)ng,
@@ -929,13 +949,17 @@ struct System {
           sb.ds[b] = sp.ds_block[b];
         }
         const T* qc = sp.nblocks() > 1 ? sp.qc[p].as<T>() : nullptr;
-        launch_simpson<T>(rho.as<double>(), sp.q[p].as<T>(), qc, sp.nblocks() == 1, sp.Ns, ng, sb, sp.phi, sp.Nref,
-                          sp.Qdev.as<double>(), fac, st);
+        // pooled density: phi / Q (canonical) or exp(mu) (grand: phi = Q exp(mu), system.jl:248-289)
+        launch_simpson<T>(rho.as<double>(), sp.q[p].as<T>(), qc, sp.nblocks() == 1, sp.Ns, ng, sb,
+                          grand ? std::exp(sp.mu_in) : sp.phi, sp.Nref,
+                          grand ? one.as<double>() : sp.Qdev.as<double>(), fac, st);
       } else {
         const int mid = sp.mids[0];
         const double vol = monomers.at(mid).first;
+        const bool grand = ensemble == 1;
         launch_point_q(grid_ptr(w, mid), vol, ng, part.as<double>(), sp.Qdev.as<double>(), st);
-        launch_point_density(grid_ptr(rho, mid), grid_ptr(w, mid), vol, sp.phi, sp.Qdev.as<double>(), ng, st);
+        launch_point_density(grid_ptr(rho, mid), grid_ptr(w, mid), vol, grand ? std::exp(sp.mu_in) : sp.phi,
+                             grand ? one.as<double>() : sp.Qdev.as<double>(), ng, st);
       }
     }
     record_ev(3);
@@ -1050,20 +1074,26 @@ struct System {
     check_pipe(last_prec);
     for (auto& sp : species) {
       sp->Q_valid = true;
-      sp->mu = std::log(sp->phi / sp->Q);  // muphi! canonical (system.jl:248-259)
+      if (ensemble == 0) {
+        sp->mu = std::log(sp->phi / sp->Q);  // muphi! canonical (system.jl:248-259)
+      } else {
+        sp->mu = sp->mu_in;  // muphi! grand: phi = Q exp(mu)
+        sp->phi = sp->Q * std::exp(sp->mu_in);
+      }
     }
   }
 
   // ---------------------------------------------------------------- residuals!(sys)
   void residuals() {
     density();
-    launch_residuals(w.as<double>(), pot.as<double>(), res.as<double>(), rho.as<double>(), monomer_set(), ng, true,
-                     part.as<double>(), sums.as<double>(), st);
+    launch_residuals(w.as<double>(), pot.as<double>(), res.as<double>(), rho.as<double>(), monomer_set(), ng,
+                     ensemble == 0, part.as<double>(), sums.as<double>(), st);  // mean-subtract: canonical only
     check_launch();
   }
 
   // field_error and free_energy from one reduction pass
   void stats(double& ferr, double& fhelm) {
+    if (ensemble == 1) fetch_Q();  // phi = Q exp(mu) enters the translational term
     launch_stats(w.as<double>(), res.as<double>(), rho.as<double>(), monomer_set(), ng, part.as<double>(),
                  stats4.as<double>(), st);
     check_launch();
@@ -1094,6 +1124,10 @@ struct System {
       const double va = monomers.at(kv.first.first).first, vb = monomers.at(kv.first.second).first;
       e += kv.second * (fr[kv.first.first] / va) * (fr[kv.first.second] / vb);
     }
+    for (auto& kv : edwards) {  // edwards.jl:49-64
+      const double v = monomers.at(kv.first).first;
+      e += kv.second / 2.0 * (fr[kv.first] / v) * (fr[kv.first] / v);
+    }
     return f + e;
   }
 
@@ -1109,7 +1143,8 @@ struct System {
     if (s[1] == 0.0) throw PFError(E_ARG, "Fields must be initialized before SCFT simulation.");
     double phisum = 0.0;
     for (auto& sp : species) phisum += sp->phi;
-    if (!isapprox(phisum, 1.0)) throw PFError(E_ARG, "Species volume fractions do not sum to unity.");
+    if (ensemble == 0 && !isapprox(phisum, 1.0))
+      throw PFError(E_ARG, "Species volume fractions do not sum to unity.");
     double charge = 0.0;
     for (int id : mon_ids) {
       double fr = 0.0;
@@ -1213,7 +1248,8 @@ struct System {
     }
     for (int k = 0; k < npr; ++k) {
       dQ[k] /= 3.0;
-      dQ[k] /= scaled(p) ? sp.Nref : sp.Q * sp.Nref;
+      // rescaled canonical chains carry 1/Q in fac[s]; grand-canonical fac[s] does not
+      dQ[k] /= (scaled(p) && ensemble == 0) ? sp.Nref : sp.Q * sp.Nref;
     }
     return dQ;
   }
@@ -1451,6 +1487,7 @@ struct System {
   void pullback_t(int p, std::vector<double>& cell_bar, std::vector<double>& nref_bar) {
     require_ready();
     if (mde != 0) throw PFError(E_UNSUPPORTED, "the pullback differentiates the RK2 propagator");
+    if (ensemble != 0) throw PFError(E_UNSUPPORTED, "the pullback differentiates the canonical ensemble");
     density_t<T>(p);
     fetch_Q();
     const int npr = cell.np(), nw = npr + 1;
@@ -1891,6 +1928,18 @@ int pf_set_adjoint_checkpoints(pf_system* sys, int every) {
     if (every < 0) throw pf::PFError(PF_EARG, "checkpoint interval must be >= 0");
     s.adj_ckpt = every;
   });
+}
+
+int pf_set_ensemble(pf_system* sys, int ensemble) {
+  return guard(sys, [&](pf::System& s) {
+    if (ensemble != 0 && ensemble != 1) throw pf::PFError(PF_EARG, "ensemble must be 0 (Canonical) or 1 (Grand)");
+    if (!s.species.empty()) throw pf::PFError(PF_ESTATE, "set the ensemble before adding species");
+    s.ensemble = ensemble;
+  });
+}
+
+int pf_set_edwards(pf_system* sys, int mid, double u) {
+  return guard(sys, [&](pf::System& s) { s.set_edwards(mid, u); });
 }
 
 int pf_set_mde(pf_system* sys, int method) {

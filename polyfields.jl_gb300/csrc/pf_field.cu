@@ -233,7 +233,7 @@ template void launch_simpson<double>(double*, const double*, const double*, bool
 
 __global__ void scale_finalize_kernel(const double* __restrict__ lf, const double* __restrict__ lb, bool rev, int Ns,
                                       const double* __restrict__ meanq, double* __restrict__ Qdev,
-                                      double* __restrict__ fac) {
+                                      double* __restrict__ fac, double qpow) {
   extern __shared__ double Lsh[];  // forward prefix L_s, s = 0..Ns, then backward L'_s
   double* Lf = Lsh;
   double* Lb = Lsh + (Ns + 1);
@@ -252,14 +252,14 @@ __global__ void scale_finalize_kernel(const double* __restrict__ lf, const doubl
   }
   __syncthreads();
   const double logQ = Lsh[2 * (Ns + 1)];
-  for (int s = threadIdx.x; s <= Ns; s += blockDim.x) fac[s] = exp(-Lf[s] - Lb[s] - logQ);
+  for (int s = threadIdx.x; s <= Ns; s += blockDim.x) fac[s] = exp(-Lf[s] - Lb[s] - qpow * logQ);
 }
 
 void launch_scale_finalize(const double* lsc_fwd, const double* lsc_bwd, bool rev, int Ns, const double* meanq,
-                           double* Qdev, double* fac, cudaStream_t st) {
+                           double* Qdev, double* fac, cudaStream_t st, bool divide_q) {
   const size_t smem = sizeof(double) * (2 * (size_t)(Ns + 1) + 1);
   if (smem > 48 * 1024) cudaFuncSetAttribute(scale_finalize_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  scale_finalize_kernel<<<1, 256, smem, st>>>(lsc_fwd, lsc_bwd, rev, Ns, meanq, Qdev, fac);
+  scale_finalize_kernel<<<1, 256, smem, st>>>(lsc_fwd, lsc_bwd, rev, Ns, meanq, Qdev, fac, divide_q ? 1.0 : 0.0);
   count_launches(1);
 }
 
@@ -350,6 +350,8 @@ __global__ void stats_kernel(const double* __restrict__ w, const double* __restr
         const double c = ms.chi[a * kMaxMon + b];
         if (c != 0.0) s3 += c * (da / ms.vol[a]) * (rho[(long)b * ng + i] / ms.vol[b]);
       }
+      const double u = ms.chi[a * kMaxMon + a];  // Edwards: (u/2) (rho_a / v_a)^2
+      if (u != 0.0) s3 += 0.5 * u * (da / ms.vol[a]) * (da / ms.vol[a]);
     }
   }
   s0 = block_sum(s0, red[0]);

@@ -179,7 +179,7 @@ void launch_stress(const StressItem<T>* items, int nitems, const T* const* src_q
 struct MonomerSet {
   int nmon;
   double vol[kMaxMon];
-  double chi[kMaxMon * kMaxMon];  // symmetric, zero diagonal
+  double chi[kMaxMon * kMaxMon];  // symmetric; off-diagonal Flory chi, diagonal Edwards u
 };
 
 // Simpson block description for one species (reference multiblock.jl:182-228).
@@ -206,9 +206,11 @@ void launch_simpson(double* rho_all, const T* q, const T* qc, bool qc_reversed, 
                     cudaStream_t st);
 // Q and the Simpson factors of a rescaled chain: L_s = sum_{t<s} lsc_fwd[t],
 // L'_s = sum_{t<Ns-s} lsc_bwd[t] (or L_{Ns-s} when rev), log Q = log(meanq) - L_Ns,
-// fac[s] = exp(-L_s - L'_s - log Q).  One block.
+// fac[s] = exp(-L_s - L'_s - log Q) (without the log Q term when !divide_q: grand-canonical
+// densities carry exp(mu) instead of 1/Q).  One block.
 void launch_scale_finalize(const double* lsc_fwd, const double* lsc_bwd, bool rev, int Ns, const double* meanq,
-                           double* Qdev, double* fac, cudaStream_t st);
+                           double* Qdev, double* fac, cudaStream_t st,
+                           bool divide_q = true);
 int launch_residuals(double* w, double* pot, double* res, const double* rho, const MonomerSet& ms, long ng,
                      bool canonical, double* part, double* sums, cudaStream_t st);
 void launch_stats(const double* w, const double* res, const double* rho, const MonomerSet& ms, long ng,

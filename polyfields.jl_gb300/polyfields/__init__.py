@@ -3,7 +3,7 @@
 The compute path is libpolyfields_gpu.so (hand-written sm_103a CUDA kernels behind the C ABI
 of include/polyfields_gpu.h); this package mirrors the reference's public API on top of it.
 """
-from .api import (AndersonUpdater, Canonical, Diblock, DomainUpdater, EulerUpdater, FieldSystem, FloryInteraction, FP32, FP64,
+from .api import (AndersonUpdater, Canonical, Diblock, DomainUpdater, EdwardsInteraction, EulerUpdater, FieldSystem, FloryInteraction, FP32, FP64,
                   Grand, Homopolymer, MomentumUpdater, Monomer, Multiblock, Point, SCFTOptions, SCFTResults, UnitCell, add_interaction,
                   add_species, chain_grid, density, field_error, fieldinit, free_energy, free_energy_bulk, loadfields,
                   residuals, savefields, scfstress, scft, scft_batch, set_interaction, setup, step,

@@ -182,6 +182,19 @@ class FloryInteraction:
         self.chis[pair] = float(chi)
 
 
+class EdwardsInteraction:
+    """src/interactions/edwards.jl:9-87: excluded volume (u/2) sum_i (rho_i / v_i)^2."""
+
+    def __init__(self):
+        self.mids = set()
+        self.uvals: Dict[int, float] = {}
+
+    def set_interaction(self, mid, u: float):
+        mid = mid.id if isinstance(mid, Monomer) else int(mid)
+        self.mids.add(mid)
+        self.uvals[mid] = float(u)
+
+
 def set_interaction(itx: FloryInteraction, alpha, beta, chi: float):
     itx.set_interaction(alpha, beta, chi)
 
@@ -229,8 +242,8 @@ class FieldSystem:
 
     def __init__(self, dims, cell: UnitCell, monomers: Sequence[Monomer] = (), ensemble: str = Canonical,
                  precision: str = FP64, mde: str = "RK2"):
-        if ensemble != Canonical:
-            raise ValueError("the GPU engine implements the canonical ensemble")
+        if ensemble not in (Canonical, Grand):
+            raise ValueError(f"unknown ensemble {ensemble}")
         mde = str(mde).lstrip(":")
         if mde not in ("RK2", "RQM4"):
             raise ValueError(f"Invalid propagator method `{mde}` for PseudoSpectralSolver.")
@@ -243,6 +256,8 @@ class FieldSystem:
         if st != L.PF_OK:
             raise L.PolyFieldsError(st, f"pf_system_create{dims}: {lib.pf_status_string(st).decode()}")
         self._h = h
+        if ensemble == Grand:
+            L.check(lib.pf_set_ensemble(h, 1), h)
         if mde == "RQM4":
             L.check(lib.pf_set_mde(h, 1), h)
         self.mde = mde
@@ -316,11 +331,15 @@ class FieldSystem:
         self.species.append(species)
         self.phi_species.append(float(val))
 
-    def add_interaction(self, itx: FloryInteraction) -> None:
-        if not isinstance(itx, FloryInteraction):
-            raise TypeError("the GPU engine implements FloryInteraction")
-        for (a, b), chi in itx.chis.items():
-            L.check(L.load().pf_set_flory(self._h, a, b, chi), self._h)
+    def add_interaction(self, itx) -> None:
+        if isinstance(itx, FloryInteraction):
+            for (a, b), chi in itx.chis.items():
+                L.check(L.load().pf_set_flory(self._h, a, b, chi), self._h)
+        elif isinstance(itx, EdwardsInteraction):
+            for mid, u in itx.uvals.items():
+                L.check(L.load().pf_set_edwards(self._h, mid, u), self._h)
+        else:
+            raise TypeError("the GPU engine implements FloryInteraction and EdwardsInteraction")
         self.interactions.append(itx)
 
     # -- hot path (system.jl)
@@ -398,7 +417,7 @@ class FieldSystem:
             out["Nref_block"].append(list(nref[k:k + n]))
             k += n
         for itx in self.interactions:
-            for pair in itx.chis:
+            for pair in getattr(itx, "chis", {}):
                 out["chi"][pair] = 0.0
         return out
 

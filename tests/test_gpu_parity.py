@@ -331,3 +331,56 @@ def test_rqm4_density_fp64(name, kw):
         assert rel(g.density[mid], o.density[mid]) < FP64_RTOL
     assert g.free_energy() == pytest.approx(o.free_energy(), rel=FP64_RTOL)
     assert np.allclose(g.scfstress(), o.scfstress(), rtol=1e-9, atol=1e-14)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_RTOL), ("fp32", FP32_RTOL)])
+def test_edwards_interaction(prec, tol):
+    """EdwardsInteraction (edwards.jl:34-87) beside a FloryInteraction: potentials, residuals,
+    free energy (the (u/2) sum (rho/v)^2 term) and bulk free energy against the oracle."""
+    def build(M, **extra):
+        A, B = M.Monomer(1, 1.0), M.Monomer(2, 1.3)
+        s = M.FieldSystem((32, 32, 1), M.UnitCell(2, "hexagonal", 8.0), monomers=[A, B], **extra)
+        s.add_species(M.Diblock(A, B, 100, 0.5, 1.0, 1.0, 100), 1.0)
+        f = M.FloryInteraction()
+        f.set_interaction(A, B, 0.25)
+        s.add_interaction(f)
+        e = M.EdwardsInteraction()
+        e.set_interaction(A, 0.6)
+        e.set_interaction(B, 0.3)
+        s.add_interaction(e)
+        M.fieldinit(s, SY.seeded_fields((1, 32, 32), [1, 2], 41, 0.3))
+        return s
+    o = build(O)
+    g = build(pf, precision=prec)
+    for mid in (1, 2):
+        assert rel(g.potentials[mid], o.potentials[mid]) < tol
+        assert rel(g.residuals[mid], o.residuals[mid]) < 10 * tol
+    assert g.free_energy() == pytest.approx(o.free_energy(), rel=tol)
+    assert g.free_energy_bulk() == pytest.approx(o.free_energy_bulk(), rel=1e-13)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_RTOL), ("fp32", 2 * FP32_RTOL)])
+def test_grand_ensemble(prec, tol):
+    """Grand ensemble (system.jl:148-157, 248-259, 332-339): add_species! values are chemical
+    potentials, phi = Q exp(mu) after each solve, no mean subtraction; a diblock, a homopolymer
+    and a point species, 2D hexagonal cell."""
+    def build(M, **extra):
+        A, B, C = M.Monomer(1, 1.0), M.Monomer(2, 1.0), M.Monomer(3, 1.0)
+        ens = O.GRAND if M is O else pf.Grand
+        s = M.FieldSystem((32, 32, 1), M.UnitCell(2, "hexagonal", 8.0), monomers=[A, B, C], ensemble=ens, **extra)
+        s.add_species(M.Diblock(A, B, 100, 0.4, 1.0, 1.0, 100), -5.8)
+        s.add_species(M.Homopolymer(A, 50, 1.0, 100), -1.3)
+        s.add_species(M.Point(C), -0.5)
+        f = M.FloryInteraction()
+        f.set_interaction(A, B, 0.2)
+        f.set_interaction(B, C, 0.1)
+        s.add_interaction(f)
+        M.fieldinit(s, SY.seeded_fields((1, 32, 32), [1, 2, 3], 43, 0.3))
+        return s
+    o = build(O)
+    g = build(pf, precision=prec)
+    for mid in (1, 2, 3):
+        assert rel(g.density[mid], o.density[mid]) < tol, mid
+        assert rel(g.residuals[mid], o.residuals[mid]) < 10 * tol, mid
+    assert g.free_energy() == pytest.approx(o.free_energy(), rel=tol)
+    assert np.allclose(g.scfstress(), o.scfstress(), rtol=1e-9 if prec == "fp64" else 2e-3, atol=1e-12)
