@@ -514,8 +514,11 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS) __maxnreg__((PlaneC
 }
 
 // ------------------------------------------------------------------ 3D: plane pass
+#ifndef PF_XY_MINB
+#define PF_XY_MINB 1
+#endif
 template <typename T, int NX, int NY>
-__global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS)
+__global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, PF_XY_MINB)
     xy_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nz, Twiddles<T> twg) {
   using C = PlaneCfg<NX, NY>;
   static_assert(NY > 1, "3D grids have Ny > 1");
