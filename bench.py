@@ -236,6 +236,15 @@ def run_gpu(args):
                 "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
                 "avg_step_us": mde_step_us}
+    # The step is issue bound before it is HBM bound: ncu counts 5.53e6 + 3.04e6 warp instructions
+    # for one chain step at 128^3 (plane + pencil pass); 152 SMs x 4 schedulers issue at most one
+    # warp instruction per cycle each at the sampled SM clock.
+    issue = None
+    if n == 128:
+        winst = 5.53e6 + 3.04e6
+        mhz = (clk or {}).get("sm_mhz") or 2070.0
+        floor_us = winst / (152 * 4 * mhz * 1e6) * 1e6
+        issue = {"warp_instructions_per_step": winst, "floor_us": floor_us, "frac": floor_us / mde_step_us}
 
     # ---- e2e through the public API with host buffers (pinned when torch is present)
     try:
@@ -281,7 +290,8 @@ def run_gpu(args):
             "mde_steps_per_s": value * nmde, "mde_steps_per_iter": nmde, "propagate_ms_per_iter": prop_step_ms,
             "density_ms_per_iter": dens_ms / args.steps, "host_ms_per_step": 1000.0 * t_host / args.steps,
             "fp64": fp64, "mixed_vs_fp64_iter_speedup": (value / fp64["iters_per_s"]) if fp64 else None,
-            "ferr": ferr, "fhelm": fhelm, "roofline": roofline, "e2e": e2e, "gpu_launches": int(launches),
+            "ferr": ferr, "fhelm": fhelm, "roofline": roofline, "issue_roofline": issue, "e2e": e2e,
+            "gpu_launches": int(launches),
             "clocks": clk, "cpu_baseline": cpu}
     print(json.dumps(line))
     return 0
