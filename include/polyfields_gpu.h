@@ -49,7 +49,9 @@ typedef struct pf_system pf_system;
 
 /* SCFTOptions (src/simulate.jl:12-19) plus the mixed-precision switch.  When
  * mixed_switch_ferr > 0 and the handle runs PF_FP32, scft switches to PF_FP64 once
- * ferr < mixed_switch_ferr and continues to ftol/stol (FP64 polish). */
+ * ferr < mixed_switch_ferr, or once the FP32 iterations have not lowered ferr by 1% for 200
+ * steps (their rounding floor lies above mixed_switch_ferr), and continues to ftol/stol (FP64
+ * polish). */
 typedef struct pf_scft_options {
   int nsteps;
   int nsout;

@@ -1,6 +1,6 @@
 """Time-to-solution of the large-blend system: plain FP64 solve vs FP32 iterations with FP64 polish.
 
-    python polyfields.jl_gb300/converge.py [--n 128] [--nsteps 4000] [--switch 1e-5] [--modes mixed,fp64]
+    python polyfields.jl_gb300/converge.py [--n 128] [--nsteps 4000] [--switch 3e-6] [--modes mixed,fp64]
         [--nhist 20] [--iter-euler 1] [--lam-euler 0.01] [--nskip 5] [--nper 20] [--fixed-cell]
         [--system blend|bcc]
 
@@ -49,7 +49,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--nsteps", type=int, default=4000)
-    ap.add_argument("--switch", type=float, default=1e-5)
+    ap.add_argument("--switch", type=float, default=3e-6)
     ap.add_argument("--ftol", type=float, default=1e-8)
     ap.add_argument("--stol", type=float, default=1e-8)
     ap.add_argument("--modes", default="mixed,fp64")

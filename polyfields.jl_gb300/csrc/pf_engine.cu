@@ -1753,6 +1753,11 @@ struct System {
       prec = 0;
       r.switch_step = 0;
     }
+    // a float32 phase that stops improving (no new minimum of ferr for kStall iterations: its
+    // rounding floor lies above mixed_switch_ferr) switches to float64 as well
+    constexpr int kStall = 200;
+    double best = ferr;
+    int best_step = 0;
     if (!converged && o.nsout > 0) printf("--------------------------------------------------------------\n");
     while (step < o.nsteps && !converged) {
       if (o.nsout > 0 && step % o.nsout == 0)
@@ -1774,10 +1779,16 @@ struct System {
         if (o.nsout > 0) printf("Converged @ step = %d: ferr = %8e, fhelm = %.5e\n", step, ferr, fhelm);
         break;
       }
-      if (mixed && prec == 1 && ferr < o.mixed_switch_ferr) {
-        prec = 0;
-        r.switch_step = step;
-        if (active == 0) anderson_restart();
+      if (mixed && prec == 1) {
+        if (ferr < 0.99 * best) {
+          best = ferr;
+          best_step = step;
+        }
+        if (ferr < o.mixed_switch_ferr || step - best_step >= kStall) {
+          prec = 0;
+          r.switch_step = step;
+          if (active == 0) anderson_restart();
+        }
       }
       step += 1;
     }

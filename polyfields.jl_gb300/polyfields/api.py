@@ -601,7 +601,8 @@ def step(updater, **kwargs) -> None:
 @dataclass
 class SCFTOptions:
     """src/simulate.jl:12-19, plus ``mixed_switch_ferr``: with an fp32 system, iterate in fp32
-    until ferr < mixed_switch_ferr, then continue in fp64 (0 disables the switch)."""
+    until ferr < mixed_switch_ferr (or until 200 fp32 iterations bring no 1% improvement),
+    then continue in fp64 (0 disables the switch)."""
     nsteps: int = 100
     nsout: int = 0
     nsave: int = 0
