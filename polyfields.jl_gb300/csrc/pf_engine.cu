@@ -40,9 +40,14 @@ struct PFError : std::runtime_error {
                         std::string("CUDA error ") + cudaGetErrorString(e_) + " at " #call);         \
   } while (0)
 
-static void check_launch() {
+// A launch error (or, with synchronous launches, a kernel fault) names the source line of
+// the check that saw it.
+#define check_launch() check_launch_at(__LINE__)
+static void check_launch_at(int line) {
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) throw PFError(E_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess)
+    throw PFError(E_CUDA, std::string("kernel launch failed (pf_engine.cu:") + std::to_string(line) +
+                              "): " + cudaGetErrorString(e));
 }
 
 // Owning device buffer.

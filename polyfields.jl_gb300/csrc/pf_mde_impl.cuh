@@ -515,7 +515,7 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS) __maxnreg__((PlaneC
 
 // ------------------------------------------------------------------ 3D: plane pass
 #ifndef PF_XY_MINB
-#define PF_XY_MINB 1
+#define PF_XY_MINB 2
 #endif
 template <typename T, int NX, int NY>
 __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, PF_XY_MINB)
