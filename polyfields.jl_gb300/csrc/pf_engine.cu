@@ -50,6 +50,16 @@ static void check_launch_at(int line) {
                               "): " + cudaGetErrorString(e));
 }
 
+// Host -> device copy ordered on stream st and complete on return.  A plain cudaMemcpy runs
+// on the legacy default stream, which does not order with the non-blocking streams the engine
+// launches on, and returns for pageable sources before its DMA has landed: a kernel on st could
+// read the destination before the data arrives.
+#define PF_H2D(dst, src, bytes, st)                                                   \
+  do {                                                                                \
+    PF_CU(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyHostToDevice, (st)));       \
+    PF_CU(cudaStreamSynchronize(st));                                                 \
+  } while (0)
+
 // Owning device buffer.
 struct DevBuf {
   void* p = nullptr;
@@ -506,7 +516,7 @@ struct System {
     {
       const double v1 = 1.0;
       one.alloc(sizeof(double));
-      PF_CU(cudaMemcpy(one.p, &v1, sizeof(double), cudaMemcpyHostToDevice));
+      PF_H2D(one.p, &v1, sizeof(double), st);
     }
     build_twiddles<double>(0);
     build_twiddles<float>(1);
@@ -567,7 +577,7 @@ struct System {
     }
     if (h.empty()) h.push_back(cx<T>(1, 0));
     twid[p].alloc(sizeof(Cx<T>) * h.size());
-    PF_CU(cudaMemcpy(twid[p].p, h.data(), sizeof(Cx<T>) * h.size(), cudaMemcpyHostToDevice));
+    PF_H2D(twid[p].p, h.data(), sizeof(Cx<T>) * h.size(), st);
   }
   template <typename T>
   Twiddles<T> tw(int p) const {
@@ -756,7 +766,7 @@ struct System {
         }
       }
       sp.ops[p].alloc(sizeof(StepOp<T>) * hops.size());
-      PF_CU(cudaMemcpy(sp.ops[p].p, hops.data(), sizeof(StepOp<T>) * hops.size(), cudaMemcpyHostToDevice));
+      PF_H2D(sp.ops[p].p, hops.data(), sizeof(StepOp<T>) * hops.size(), st);
       const StepOp<T>* ops = sp.ops[p].as<StepOp<T>>();
       Cx<T>* kb0 = nullptr;
       Cx<T>* kb1 = nullptr;
@@ -806,7 +816,7 @@ struct System {
     job_steps.clear();
     for (const auto& j : hjobs) job_steps.push_back(j.nsteps);
     jobs[p].alloc(sizeof(ChainJob<T>) * std::max(1, njobs));
-    if (njobs) PF_CU(cudaMemcpy(jobs[p].p, hjobs.data(), sizeof(ChainJob<T>) * njobs, cudaMemcpyHostToDevice));
+    if (njobs) PF_H2D(jobs[p].p, hjobs.data(), sizeof(ChainJob<T>) * njobs, st);
     jobs_dirty[p] = false;
   }
 
@@ -845,14 +855,14 @@ struct System {
         sp.rq_ld2.push_back(sp.ld2[b]->as<double>());
       }
       sp.rq_ops.alloc(sizeof(StepOp<double>) * hops.size());
-      PF_CU(cudaMemcpy(sp.rq_ops.p, hops.data(), sp.rq_ops.bytes, cudaMemcpyHostToDevice));
+      PF_H2D(sp.rq_ops.p, hops.data(), sp.rq_ops.bytes, st);
       const StepOp<double>* ops = sp.rq_ops.as<StepOp<double>>();
       for (int b = 0; b < nb; ++b) {
         hj.push_back(ChainJob<double>{X, ops + 3 * b, kb, nullptr, nullptr, 0, +1, 1, 0});
         hj.push_back(ChainJob<double>{Y, ops + 3 * b + 1, kb, nullptr, nullptr, 0, +1, 2, 0});
       }
       sp.rq_jobs.alloc(sizeof(ChainJob<double>) * hj.size());
-      PF_CU(cudaMemcpy(sp.rq_jobs.p, hj.data(), sp.rq_jobs.bytes, cudaMemcpyHostToDevice));
+      PF_H2D(sp.rq_jobs.p, hj.data(), sp.rq_jobs.bytes, st);
     }
   }
   // x -> y by one RQM4 step of block b: y = (4 q2 - q1) / 3
@@ -1644,7 +1654,7 @@ struct System {
                                      scaled(p) ? segcsc.as<float>() : nullptr,
                                      scaled(p) ? seglsc.as<double>() : nullptr, 0, +1, std::min(K, Ns - c * K), 0});
         segjobs.alloc(sizeof(ChainJob<T>) * sj.size());
-        PF_CU(cudaMemcpy(segjobs.p, sj.data(), segjobs.bytes, cudaMemcpyHostToDevice));
+        PF_H2D(segjobs.p, sj.data(), segjobs.bytes, st);
       }
       // propagators of segment c of chain ch: B[j] = step c*K + j of that chain, from its checkpoint
       auto recompute = [&](int ch, int c, const T* start) {
