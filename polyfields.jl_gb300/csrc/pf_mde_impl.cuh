@@ -719,10 +719,13 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
   Cx<T>* ktiles = reinterpret_cast<Cx<T>*>(sbase);                    // [S][TPC] tiles of KB bytes
   T* ltiles = reinterpret_cast<T*>(sbase + (size_t)S * TPC * Z::KB);  // [S][TPC] tiles of LB bytes
   __shared__ __align__(8) uint64_t full[S];
-  __shared__ Cx<T> twz[tw_total<NZ>()];
+  __shared__ __align__(16) Cx<T> twz[tw_total<NZ>()];
   const int nrounds = (ntiles + TPC - 1) / TPC;
   const int nk = (int)blockIdx.x < nrounds ? (nrounds - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-  stage<T>(twz, twg.z, tw_total<NZ>());
+  // twiddles ride on the first stage's bulk copies when the table is 16-byte aligned
+  constexpr unsigned TWB = (unsigned)(sizeof(Cx<T>) * tw_total<NZ>());
+  const bool tw_bulk = (TWB % 16 == 0) && ((reinterpret_cast<uintptr_t>(twg.z) & 15) == 0);
+  if (!tw_bulk) stage<T>(twz, twg.z, tw_total<NZ>());
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) mbar_init(&full[s], 1);
     fence_mbar_init();
@@ -732,7 +735,9 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
   auto issue = [&](int k) {  // thread 0: fill stage k % S with round k of this CTA
     const int s = k % S, r = (int)blockIdx.x + k * (int)gridDim.x;
     const int nt = min(TPC, ntiles - r * TPC);
-    mbar_expect_tx(&full[s], (unsigned)(nt * (Z::KB + Z::LB)));
+    const bool tw = k == 0 && tw_bulk;
+    mbar_expect_tx(&full[s], (unsigned)(nt * (Z::KB + Z::LB)) + (tw ? TWB : 0u));
+    if (tw) bulk_load(twz, twg.z, TWB, &full[s]);
     for (int j = 0; j < nt; ++j) {
       const int tile = r * TPC + j;
       tma_load_2d(ktiles + (size_t)(s * TPC + j) * (Z::KB / Z::E), &kmap, tile * 16, 0, &full[s]);
