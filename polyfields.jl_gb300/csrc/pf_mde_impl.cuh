@@ -576,7 +576,9 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, PF_XY_MINB)
 // zrow_perm, that spreads each group's accesses over the banks under the swizzle); after LD and
 // the inverse transform the tile goes back to global memory with one TMA store.  Each CTA runs
 // several tiles through STAGES buffers, so copies of the next tiles overlap the transforms.
-static __device__ int g_pipe_status;  // nonzero: a pipeline wait gave up (the launch's output is invalid)
+// Nonzero when a bounded wait of the pencil pipeline gave up; that launch's output is invalid.
+// Read and cleared by the host.
+static __device__ int g_pipe_status;
 
 template <typename T, int NZ>
 struct ZPipe {
