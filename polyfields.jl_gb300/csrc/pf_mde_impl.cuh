@@ -169,21 +169,48 @@ struct BARegs {
   Cx<T> v[JoinBA<N>::BPT][JoinBA<N>::R];
 };
 
-// Column transforms, inverse, order A: from the [kx][ky] global plane kin into
-// S[y Kx + kx].  Group c < Kx handles column c.  The caller syncs the CTA afterwards.
+// Inputs of the first column pass (inverse, order A) of one group: column c of the [kx][ky]
+// global plane.
+template <typename T, int NY>
+struct ColIn {
+  using P0 = PassOf<T, true, NY, 0, 0>;
+  Cx<T> v[P0::BPT][Order<NY, 0>::radix(0)];
+};
+
+template <typename T>
+__device__ __forceinline__ Cx<T> ld_l2(const Cx<T>* p) {
+  if constexpr (sizeof(T) == 4) {
+    const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+    return cx<T>(v.x, v.y);
+  } else {
+    const double2 v = __ldcg(reinterpret_cast<const double2*>(p));
+    return cx<T>(v.x, v.y);
+  }
+}
+
+// Issue the loads of the first column pass from the global plane kin (cached in L2 only: the
+// plane is read once).  Independent of shared memory, so it can run before the twiddles are
+// staged.
 template <typename T, int NX, int NY>
-__device__ __forceinline__ void y_inverse_from_global(Cx<T>* S, const Cx<T>* __restrict__ kin, const Cx<T>* twy) {
+__device__ __forceinline__ void y_inverse_load(ColIn<T, NY>& in, const Cx<T>* __restrict__ kin) {
+  using C = PlaneCfg<NX, NY>;
+  const int c = group_index<C::GY, C::SC>(threadIdx.x / C::GY), g = threadIdx.x % C::GY;
+  if (c < C::KX) ColIn<T, NY>::P0::load(in.v, g, [&](int i) { return ld_l2<T>(kin + c * NY + i); });
+}
+
+// Column transforms, inverse, order A, from the loaded inputs into S[y Kx + kx].  Group c < Kx
+// handles column c.  The caller syncs the CTA afterwards.
+template <typename T, int NX, int NY>
+__device__ __forceinline__ void y_inverse_from_loaded(Cx<T>* S, ColIn<T, NY>& in, const Cx<T>* twy) {
   using C = PlaneCfg<NX, NY>;
   constexpr int P = Order<NY, 0>::P;
   const int c = group_index<C::GY, C::SC>(threadIdx.x / C::GY), g = threadIdx.x % C::GY;
   const bool active = c < C::KX;
   Cx<T>* col = S + (active ? c : 0);
-  using P0 = PassOf<T, true, NY, 0, 0>;
-  Cx<T> v[P0::BPT][Order<NY, 0>::radix(0)];
+  using P0 = typename ColIn<T, NY>::P0;
   if (active) {
-    P0::load(v, g, [&](int i) { return kin[c * NY + i]; });
-    P0::compute(v, g, twy);
-    P0::store(v, g, [&](int i, const Cx<T>& x) { col[(P > 1 ? pswz<NY>(i) : i) * C::KX] = x; });
+    P0::compute(in.v, g, twy);
+    P0::store(in.v, g, [&](int i, const Cx<T>& x) { col[(P > 1 ? pswz<NY>(i) : i) * C::KX] = x; });
   }
   __syncwarp();
   smem_passes<T, true, NY, 0, 1, P, true, false>(col, C::KX, g, twy, active);
@@ -517,6 +544,7 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS) __maxnreg__((PlaneC
 #ifndef PF_XY_MINB
 #define PF_XY_MINB 2
 #endif
+
 template <typename T, int NX, int NY>
 __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, PF_XY_MINB)
     xy_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nz, Twiddles<T> twg) {
@@ -527,8 +555,6 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, PF_XY_MINB)
   const ChainJob<T> job = jobs[blockIdx.y];
   if (t > job.nsteps) return;
   __shared__ Cx<T> twx[C::TWX], twy[C::TWY];
-  stage<T>(twx, twg.x, C::TWX);
-  stage<T>(twy, twg.y, C::TWY);
   const int z = blockIdx.x;
   const long ng = (long)C::NP * nz;
   const bool finish = t >= 1;
@@ -537,19 +563,29 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, PF_XY_MINB)
   const bool xact = p < C::NPAIR;
   const int c = group_index<C::GY, C::SC>(threadIdx.x / C::GY), gy = threadIdx.x % C::GY;
   const bool yact = c < C::KX;
+  // The global reads that do not depend on shared memory go out before the twiddle barrier, so
+  // that their latencies overlap: the step operator, the rescale factor and the input plane
+  // (+0.7% iterations/s at 128^3 over loading them after the barrier).
+  const T* lw_cur = nullptr;
+  const T* lw_next = nullptr;
+  T cs = (T)1;
+  ColIn<T, NY> in;
+  if (finish) {
+    lw_cur = job.ops[t - 1].lw + (long)z * C::NP;
+    if (job.csc) cs = (T)job.csc[t - 1];
+    y_inverse_load<T, NX, NY>(in, job.kbuf + (long)z * C::NKP);
+  }
+  if (start) lw_next = job.ops[t].lw + (long)z * C::NP;
+  stage<T>(twx, twg.x, C::TWX);
+  stage<T>(twy, twg.y, C::TWY);
   __syncthreads();
   XRegs<T, NX> r;
   if (finish) {
-    y_inverse_from_global<T, NX, NY>(S, job.kbuf + (long)z * C::NKP, twy);
+    y_inverse_from_loaded<T, NX, NY>(S, in, twy);
     __syncthreads();
     x_inverse_to_regs<T, NX, NY>(S, twx, r, p, gx, xact);
-    const StepOp<T> op = job.ops[t - 1];
     const int s_out = job.s0 + job.dir * t;
-    const T* lw_next = start ? job.ops[t].lw + (long)z * C::NP : nullptr;
-    const T cs = job.csc ? (T)job.csc[t - 1] : (T)1;
-    if (xact)
-      finish_regs<T, NX, NY>(r, p, gx, op.lw + (long)z * C::NP, lw_next, job.hist + (long)s_out * ng + (long)z * C::NP,
-                             cs);
+    if (xact) finish_regs<T, NX, NY>(r, p, gx, lw_cur, lw_next, job.hist + (long)s_out * ng + (long)z * C::NP, cs);
   } else if (xact) {
     load_regs<T, NX, NY>(r, p, gx, job.ops[0].lw + (long)z * C::NP, job.hist + (long)job.s0 * ng + (long)z * C::NP);
   }
