@@ -32,6 +32,7 @@
 #include "pf_tma.cuh"
 #include <cudaTypedefs.h>
 #include <stdexcept>
+#include <utility>
 
 namespace pf {
 
@@ -545,6 +546,7 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS) __maxnreg__((PlaneC
 #define PF_XY_MINB 2
 #endif
 
+
 template <typename T, int NX, int NY>
 __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, PF_XY_MINB)
     xy_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nz, Twiddles<T> twg) {
@@ -563,21 +565,22 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, PF_XY_MINB)
   const bool xact = p < C::NPAIR;
   const int c = group_index<C::GY, C::SC>(threadIdx.x / C::GY), gy = threadIdx.x % C::GY;
   const bool yact = c < C::KX;
-  // The global reads that do not depend on shared memory go out before the twiddle barrier, so
-  // that their latencies overlap: the step operator, the rescale factor and the input plane
-  // (+0.7% iterations/s at 128^3 over loading them after the barrier).
+  // Launched as a programmatic dependent of the previous pencil pass: what does not depend on
+  // that pass (the step operators, the twiddles) is read before grid_dep_wait, overlapping the
+  // pencil pass's tail; the spectra and the rescale factor after it.
   const T* lw_cur = nullptr;
   const T* lw_next = nullptr;
   T cs = (T)1;
   ColIn<T, NY> in;
-  if (finish) {
-    lw_cur = job.ops[t - 1].lw + (long)z * C::NP;
-    if (job.csc) cs = (T)job.csc[t - 1];
-    y_inverse_load<T, NX, NY>(in, job.kbuf + (long)z * C::NKP);
-  }
+  if (finish) lw_cur = job.ops[t - 1].lw + (long)z * C::NP;
   if (start) lw_next = job.ops[t].lw + (long)z * C::NP;
   stage<T>(twx, twg.x, C::TWX);
   stage<T>(twy, twg.y, C::TWY);
+  grid_dep_wait();  // the pencil pass of step t-1 (spectra, rescale factor) has completed
+  if (finish) {
+    if (job.csc) cs = (T)job.csc[t - 1];
+    y_inverse_load<T, NX, NY>(in, job.kbuf + (long)z * C::NKP);
+  }
   __syncthreads();
   XRegs<T, NX> r;
   if (finish) {
@@ -594,6 +597,7 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, PF_XY_MINB)
     __syncthreads();
     BARegs<T, NY> w;
     y_forward_to_regs<T, NX, NY>(S, twy, w, c, gy, yact);
+    grid_dep_launch();  // the pencil pass may be scheduled; it waits for these stores
     if (yact) {
       Cx<T>* dst = job.kbuf + (long)z * C::NKP + c * NY;
 #pragma unroll
@@ -769,6 +773,7 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
     fence_mbar_init();
   }
   __syncthreads();
+  grid_dep_wait();  // the plane pass that wrote this step's spectra has completed
   const uint64_t keep = l2_evict_last();  // LD is read by every step of the chain's block
   auto issue = [&](int k) {  // thread 0: fill stage k % S with round k of this CTA
     const int s = k % S, r = (int)blockIdx.x + k * (int)gridDim.x;
@@ -799,6 +804,7 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
       break;
     }
     waited = k + 1;
+    if (k == nk - 1) grid_dep_launch();  // last round: the next plane pass may be scheduled
     const int tile = r * TPC + slot;
     const bool active = tile < ntiles;
     Cx<T>* kt = ktiles + (size_t)(s * TPC + slot) * (Z::KB / Z::E);
@@ -1205,6 +1211,24 @@ static void make_zmaps(CUtensorMap* km, CUtensorMap* lm, const Cx<T>* kbuf, cons
   }
 }
 
+// Launch on st; with pdl the launch may begin while the previous kernel on st finishes (its
+// reads of that kernel's results wait in grid_dep_wait).
+template <typename... KArgs, typename... Args>
+static void launch_on(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl,
+                      Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 // rounds (stages of tiles) per CTA of the pencil pipeline
 #ifndef PF_ZRPC
 #define PF_ZRPC 2
@@ -1230,7 +1254,8 @@ static void launch_z_pipe(const ChainHost<T>& h, int t, int nkp, double ng, cons
   int grid = (nrounds + kZRoundsPerCta - 1) / kZRoundsPerCta;
   if (grid > grid_cap) grid = grid_cap;
   if (grid < 1) grid = 1;
-  z_pipe_kernel<T, NZ><<<grid, Z::THREADS, Z::SMEM, st>>>(km, lm, h.csc, h.lsc, t, ntiles, ng, tw);
+  launch_on(z_pipe_kernel<T, NZ>, dim3(grid), dim3(Z::THREADS), Z::SMEM, st, true, km, lm, h.csc, h.lsc, t,
+            ntiles, ng, tw);
   count_launches(1);
 }
 
@@ -1282,7 +1307,8 @@ static void chains_shape(const ChainJob<T>* jobs, int njobs, int maxsteps, int n
     auto run_job = [&](int j, cudaStream_t sj) {
       const int ns = hosts[j].nsteps;
       for (int t = 0; t <= ns; ++t) {
-        xy_step_kernel<T, NX, NY><<<dim3(nz, 1), C::THREADS, sp, sj>>>(jobs + j, t, nz, tw);
+        launch_on(xy_step_kernel<T, NX, NY>, dim3(nz, 1), dim3(C::THREADS), sp, sj, t > 0, jobs + j,
+                  t, nz, tw);
         count_launches(1);
         if (t < ns) z_pipe_dispatch<T>(nz, hosts[j], t, C::NKP, ng, tw, sj);
       }

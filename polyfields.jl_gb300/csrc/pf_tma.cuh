@@ -124,4 +124,11 @@ __device__ __forceinline__ void bulk_wait() {
   asm volatile("cp.async.bulk.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Programmatic dependent launch.  grid_dep_wait blocks until the grids this launch depends on
+// have completed and their writes are visible (it returns at once for a launch without a
+// programmatic dependency); grid_dep_launch lets the next launch on the stream be scheduled
+// once every CTA of this grid has called it or exited.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 }  // namespace pf
