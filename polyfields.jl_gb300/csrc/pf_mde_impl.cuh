@@ -547,6 +547,7 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS) __maxnreg__((PlaneC
 #endif
 
 
+
 template <typename T, int NX, int NY>
 __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, PF_XY_MINB)
     xy_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nz, Twiddles<T> twg) {
@@ -804,7 +805,6 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
       break;
     }
     waited = k + 1;
-    if (k == nk - 1) grid_dep_launch();  // last round: the next plane pass may be scheduled
     const int tile = r * TPC + slot;
     const bool active = tile < ntiles;
     Cx<T>* kt = ktiles + (size_t)(s * TPC + slot) * (Z::KB / Z::E);
@@ -826,6 +826,7 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
           w.v[b][tt] = cx<T>(w.v[b][tt].x * f, w.v[b][tt].y * f);
         }
     }
+    if (k == nk - 1) grid_dep_launch();  // last round: the next plane pass may be scheduled
     ztile_inverse<T, NZ>(kt, m, g, twz, w, active);
     fence_async_smem();
     __syncthreads();
