@@ -463,6 +463,9 @@ struct System {
     int nhist = 50, iter = 0, iter_hist = 0, iter_euler = 1, base = 0;
     double lam = 0.0, lam_euler = 0.01;
     DevBuf res_hist, field_hist;
+    // gram_p[a * nslot + b] = res(slot a) . res(slot b) for the slots of the window, gram_t
+    // the current residual's products with the window (launch_gram_cached)
+    DevBuf gram_p, gram_t;
     void reset() {
       exists = is_setup = false;
       nhist = 50;
@@ -473,6 +476,8 @@ struct System {
       lam_euler = 0.01;
       res_hist.release();
       field_hist.release();
+      gram_p.release();
+      gram_t.release();
     }
   } and_;
   // EulerUpdater (kind 1, method 0 PEC / 1 PECE) and MomentumUpdater (kind 2, method 0 MOM,
@@ -1305,6 +1310,8 @@ struct System {
     const size_t slot = sizeof(double) * nmon() * ng;
     and_.res_hist.alloc(slot * (and_.nhist + 1));
     and_.field_hist.alloc(slot * (and_.nhist + 1));
+    and_.gram_p.alloc(sizeof(double) * kMaxHist * kMaxHist);
+    and_.gram_t.alloc(sizeof(double) * kMaxHist);
     PF_CU(cudaMemsetAsync(and_.res_hist.p, 0, and_.res_hist.bytes, st));
     PF_CU(cudaMemsetAsync(and_.field_hist.p, 0, and_.field_hist.bytes, st));
     and_.base = 0;
@@ -1388,23 +1395,36 @@ struct System {
     const long nall = (long)nmon() * ng;
     residuals();
     PF_CU(cudaMemcpyAsync(hist_slot(A.res_hist, ih), res.p, sizeof(double) * nall, cudaMemcpyDeviceToDevice, st));
+    HistPtrs h{};
+    for (int j = 0; j <= ih; ++j) {
+      h.res[j] = hist_slot(A.res_hist, j);
+      h.field[j] = hist_slot(A.field_hist, j);
+    }
+    // U and V from the current residual's products with the window and the cached pair
+    // products of the older entries; every iteration (Euler warm-up included) adds its row, so
+    // the cache covers every pair of the window
+    int* flag = status.as<int>() + 1;
+    launch_gram_cached(h, res.as<double>(), ih, nall, A.gram_p.as<double>(), A.nhist + 1, A.base, part.as<double>(),
+                       A.gram_t.as<double>(), packed.as<double>(), flag, st);
     if (it <= A.iter_euler) {
       launch_axpy(w.as<double>(), res.as<double>(), A.lam_euler, nall, st);
     } else {
-      HistPtrs h{};
-      for (int j = 0; j <= ih; ++j) {
-        h.res[j] = hist_slot(A.res_hist, j);
-        h.field[j] = hist_slot(A.field_hist, j);
-      }
-      launch_gram(h, ih, nall, part.as<double>(), packed.as<double>(), st);
       launch_solve(packed.as<double>(), ih, cn.as<double>(), status.as<int>(), st);
       check_launch();
-      int sv = 0;
-      PF_CU(cudaMemcpyAsync(&sv, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+      int sv[2] = {0, 0};
+      PF_CU(cudaMemcpyAsync(sv, status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
       PF_CU(cudaStreamSynchronize(st));
-      if (sv != 0)
+      if (sv[1] != 0) {
+        // cancellation guard of the expanded sums: sum U and V directly
+        launch_gram(h, ih, nall, part.as<double>(), packed.as<double>(), st);
+        launch_solve(packed.as<double>(), ih, cn.as<double>(), status.as<int>(), st);
+        check_launch();
+        PF_CU(cudaMemcpyAsync(sv, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        PF_CU(cudaStreamSynchronize(st));
+      }
+      if (sv[0] != 0)
         throw PFError(E_SINGULAR, "Error inverting Umn matrix on iteration " + std::to_string(it) +
-                                      ": SingularException(" + std::to_string(sv) + ")");
+                                      ": SingularException(" + std::to_string(sv[0]) + ")");
       launch_mix(w.as<double>(), h, ih, cn.as<double>(), A.lam, nall, st);
     }
     check_launch();

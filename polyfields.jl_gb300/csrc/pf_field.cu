@@ -266,12 +266,19 @@ void launch_scale_finalize(const double* lsc_fwd, const double* lsc_bwd, bool re
 // ------------------------------------------------------------------ residuals
 // pot_a = sum_b chi_ab rho_b / v_b ; eta = (sum rho - 1 + sum_a (w_a - pot_a)) / nmon ;
 // res_a = pot_a + eta - w_a.  Partials: sum w_a (v = a), sum res_a (v = nmon + a).
+// NM = the monomer count (compile-time, so the per-point arrays stay in registers).
+template <int NM>
 __global__ void residual_kernel(const double* __restrict__ w, double* __restrict__ pot, double* __restrict__ res,
                                 const double* __restrict__ rho, MonomerSet ms, long ng, double* __restrict__ part) {
   __shared__ double red[2 * kMaxMon][32];
-  const int nm = ms.nmon;
-  double sw[kMaxMon], sr[kMaxMon];
+  constexpr int nm = NM;
+  double sw[kMaxMon], sr[kMaxMon], ivol[kMaxMon];
   for (int a = 0; a < kMaxMon; ++a) sw[a] = sr[a] = 0.0;
+  // per-thread reciprocals: a float64 division is a long FP64 instruction sequence, and the
+  // grid loop would otherwise run nm^2 + 1 of them per point (identical results for the
+  // usual unit volumes and a power-of-two monomer count)
+  for (int a = 0; a < nm; ++a) ivol[a] = 1.0 / ms.vol[a];
+  const double inm = 1.0 / (double)nm;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ng; i += (long)gridDim.x * blockDim.x) {
     double r[kMaxMon], wv[kMaxMon], p[kMaxMon];
     double rhosum = 0.0;
@@ -285,12 +292,12 @@ __global__ void residual_kernel(const double* __restrict__ w, double* __restrict
       double pa = 0.0;
       for (int b = 0; b < nm; ++b) {
         const double c = ms.chi[a * kMaxMon + b];
-        if (c != 0.0) pa += c * (r[b] / ms.vol[b]);
+        if (c != 0.0) pa += c * (r[b] * ivol[b]);
       }
       p[a] = pa;
       eta += wv[a] - pa;
     }
-    eta /= (double)nm;
+    eta *= inm;
     for (int a = 0; a < nm; ++a) {
       const double ra = p[a] + eta - wv[a];
       pot[(long)a * ng + i] = p[a];
@@ -323,7 +330,16 @@ __global__ void meansub_kernel(double* __restrict__ w, double* __restrict__ res,
 int launch_residuals(double* w, double* pot, double* res, const double* rho, const MonomerSet& ms, long ng,
                      bool canonical, double* part, double* sums, cudaStream_t st) {
   const int nb = red_blocks(ng);
-  residual_kernel<<<nb, 256, 0, st>>>(w, pot, res, rho, ms, ng, part);
+  switch (ms.nmon) {
+#define PF_RES(N)                                                          \
+  case N:                                                                  \
+    residual_kernel<N><<<nb, 256, 0, st>>>(w, pot, res, rho, ms, ng, part); \
+    break;
+    PF_RES(1) PF_RES(2) PF_RES(3) PF_RES(4) PF_RES(5) PF_RES(6) PF_RES(7) PF_RES(8)
+#undef PF_RES
+    default:
+      return E_ARG;
+  }
   count_launches(1);
   if (canonical) {
     reduce_parts(part, nb, 2 * ms.nmon, sums, (double)ng, st);
@@ -455,6 +471,97 @@ void launch_gram(const HistPtrs& h, int ih, long n_all, double* part, double* ou
   reduce_parts(part, (int)nb, nout, out, 1.0, st);
 }
 
+// Products of the current residual with the history: t[j] = r . res[j] for logical j = 0..nj-1
+// (res[nj-1] is the copy of r).  Blocks write partials part[block * nj + j], in a fixed order.
+constexpr int kDotChunk = 8;
+__global__ void __launch_bounds__(256) hist_dots_kernel(HistPtrs h, const double* __restrict__ r, int nj, long n,
+                                                        double* __restrict__ part) {
+  __shared__ double red[kDotChunk][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j0 = 0; j0 < nj; j0 += kDotChunk) {
+    const int nc = min(kDotChunk, nj - j0);
+    const double* hp[kDotChunk];
+    double acc[kDotChunk];
+#pragma unroll
+    for (int k = 0; k < kDotChunk; ++k) {
+      hp[k] = h.res[j0 + (k < nc ? k : 0)];
+      acc[k] = 0.0;
+    }
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+      const double rv = r[i];
+#pragma unroll
+      for (int k = 0; k < kDotChunk; ++k)
+        if (k < nc) acc[k] = fma(rv, hp[k][i], acc[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < kDotChunk; ++k) {
+      const double v = warp_sum(acc[k]);
+      if (lane == 0) red[k][wid] = v;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < nc) {
+      double v = 0.0;
+      for (int q = 0; q < nw; ++q) v += red[threadIdx.x][q];
+      part[(long)blockIdx.x * nj + j0 + threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// Gram update from cached products.  P[a * nslot + b] = res(slot a) . res(slot b) for every pair
+// of physical slots in the history window (slot of logical j = (base + j) % nslot); t[j] = r . res[j].
+// Stores the current slot's row and column of P, then the packed U and V of gram_kernel from
+//   U[m][n] = t[ih] - t[ih-1-m] - t[ih-1-n] + P[a_m][a_n],   V[m] = t[ih] - t[ih-1-m]
+// (d_m = r - res[ih-1-m]; the same sums expanded).  flag = 1 when a diagonal U[m][m] is not
+// positive or is below (|r| + |res[ih-1-m]|)^2 / kGramCancel, where the expansion's rounding could
+// exceed ~kGramCancel ulps of U[m][m]: the caller then sums U and V directly (gram_kernel).
+constexpr double kGramCancel = 1.0e3;
+__global__ void gram_assemble_kernel(double* __restrict__ P, int nslot, int base, const double* __restrict__ t, int ih,
+                                     double* __restrict__ packed, int* __restrict__ flag) {
+  __shared__ double ts[kMaxHist];
+  __shared__ int bad;
+  const int c = (base + ih) % nslot;
+  for (int j = threadIdx.x; j <= ih; j += blockDim.x) ts[j] = t[j];
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int j = threadIdx.x; j <= ih; j += blockDim.x) {
+    const int a = (base + j) % nslot;
+    P[(long)c * nslot + a] = ts[j];
+    P[(long)a * nslot + c] = ts[j];
+  }
+  __syncthreads();
+  const int npair = ih * (ih + 1) / 2;
+  const double rr = ts[ih];
+  for (int o = threadIdx.x; o < npair; o += blockDim.x) {
+    int m = 0, rem = o;
+    while (rem >= ih - m) {
+      rem -= ih - m;
+      ++m;
+    }
+    const int n = m + rem;
+    const int am = (base + ih - 1 - m) % nslot, an = (base + ih - 1 - n) % nslot;
+    const double u = (rr - ts[ih - 1 - m]) - (ts[ih - 1 - n] - P[(long)am * nslot + an]);
+    packed[o] = u;
+    if (m == n) {
+      const double scale = sqrt(rr) + sqrt(P[(long)am * nslot + am]);
+      if (!(u > 0.0) || !(scale * scale <= kGramCancel * u)) bad = 1;
+    }
+  }
+  for (int m = threadIdx.x; m < ih; m += blockDim.x) packed[npair + m] = rr - ts[ih - 1 - m];
+  __syncthreads();
+  if (threadIdx.x == 0) *flag = bad;
+}
+
+void launch_gram_cached(const HistPtrs& h, const double* r, int ih, long n_all, double* P, int nslot, int base,
+                        double* part, double* t, double* packed, int* flag, cudaStream_t st) {
+  const int nb = red_blocks(n_all);
+  hist_dots_kernel<<<nb, 256, 0, st>>>(h, r, ih + 1, n_all, part);
+  count_launches(1);
+  reduce_parts(part, nb, ih + 1, t, 1.0, st);
+  gram_assemble_kernel<<<1, 256, 0, st>>>(P, nslot, base, t, ih, packed, flag);
+  count_launches(1);
+}
+
 // LU with partial pivoting, explicit inverse, Cn = inv(U) V (the inv!(lu!(Umn)) * Vm of
 // anderson.jl:184-189).  status = k+1 when pivot k is exactly zero (LAPACK info > 0).
 __global__ void solve_kernel(const double* __restrict__ packed, int n, double* __restrict__ Cn, int* status) {
@@ -552,22 +659,32 @@ void launch_solve(const double* packed, int ih, double* Cn, int* status, cudaStr
   count_launches(1);
 }
 
-// w = W + lam D,  W = w + sum_nn Cn[nn-1] (f[ih-nn] - f[ih]),  D = r + sum_nn Cn[nn-1] (r[ih-nn] - r)
+// w = W + lam D,  W = w + sum_nn Cn[nn-1] (f[ih-nn] - f[ih]),  D = r + sum_nn Cn[nn-1] (r[ih-nn] - r).
+// Evaluated with the coefficients gathered, W = (w - C f[ih]) + sum c f[ih-nn] and
+// D = (1 - C) r + sum c r[ih-nn] (C = sum c): two FP64 FMAs per history entry and point instead
+// of two subtractions and two FMAs.
 __global__ void mix_kernel(double* __restrict__ w, HistPtrs h, int ih, const double* __restrict__ Cn, double lam,
                            long n) {
   __shared__ double c[kMaxHist];
+  __shared__ double csum;
   for (int j = threadIdx.x; j < ih; j += blockDim.x) c[j] = Cn[j];
   __syncthreads();
+  if (threadIdx.x == 0) {
+    double cs = 0.0;
+    for (int j = 0; j < ih; ++j) cs += c[j];
+    csum = cs;
+  }
+  __syncthreads();
+  const double C = csum, om = 1.0 - csum;
   const double* r = h.res[ih];
   const double* f = h.field[ih];
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const double ri = r[i], fi = f[i];
-    double W = w[i], D = ri;
+    double W = fma(-C, f[i], w[i]), D = om * r[i];
     for (int nn = 1; nn <= ih; ++nn) {
-      W += c[nn - 1] * (h.field[ih - nn][i] - fi);
-      D += c[nn - 1] * (h.res[ih - nn][i] - ri);
+      W = fma(c[nn - 1], h.field[ih - nn][i], W);
+      D = fma(c[nn - 1], h.res[ih - nn][i], D);
     }
-    w[i] = W + lam * D;
+    w[i] = fma(lam, D, W);
   }
 }
 

@@ -221,6 +221,10 @@ struct HistPtrs {
   const double* field[kMaxHist];
 };
 void launch_gram(const HistPtrs& h, int ih, long n_all, double* part, double* out, cudaStream_t st);
+// The packed U, V of launch_gram from the cached history products P (nslot x nslot, physical
+// slots, updated here with the current residual's row); flag = 1 asks for launch_gram instead.
+void launch_gram_cached(const HistPtrs& h, const double* r, int ih, long n_all, double* P, int nslot, int base,
+                        double* part, double* t, double* packed, int* flag, cudaStream_t st);
 void launch_solve(const double* packed, int ih, double* Cn, int* status, cudaStream_t st);
 void launch_mix(double* w, const HistPtrs& h, int ih, const double* Cn, double lam, long n_all, cudaStream_t st);
 
