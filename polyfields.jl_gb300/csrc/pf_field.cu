@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(256) simpson_kernel(double* __restrict__ rho_a
   const long nv = ng / W;
   const V* q4 = reinterpret_cast<const V*>(q);
   const V* qc4 = reinterpret_cast<const V*>(rev ? q : qc);
+  const bool sym = rev && blk.nblocks == 1 && blk.bgn[0] == 0 && blk.end[0] == Ns && Ns % 2 == 0 && Ns >= 2;
   for (long iv = blockIdx.x * (long)blockDim.x + threadIdx.x; iv < nv; iv += (long)gridDim.x * blockDim.x) {
     double bval[kMaxMon * 2][W];
     for (int b = 0; b < blk.nblocks; ++b) {
@@ -190,12 +191,24 @@ __global__ void __launch_bounds__(256) simpson_kernel(double* __restrict__ rho_a
           else acc[k].add(v);
         }
       };
-      term(s0, (T)1, true);
-      term(s1, (T)1, false);
+      if (sym) {
+        // symmetric chain in one block: the integrand at s and Ns - s is the same product
+        // (fac is symmetric too), so each mirrored pair is read once and counted twice
+        const int h = Ns / 2;
+        term(0, (T)2, true);
 #pragma unroll 4
-      for (int s = s0 + 1; s < s1; s += 2) term(s, (T)4, false);
+        for (int s = 1; s < h; s += 2) term(s, (T)8, false);
 #pragma unroll 4
-      for (int s = s0 + 2; s < s1 - 1; s += 2) term(s, (T)2, false);
+        for (int s = 2; s < h; s += 2) term(s, (T)4, false);
+        term(h, (h & 1) ? (T)4 : (T)2, false);
+      } else {
+        term(s0, (T)1, true);
+        term(s1, (T)1, false);
+#pragma unroll 4
+        for (int s = s0 + 1; s < s1; s += 2) term(s, (T)4, false);
+#pragma unroll 4
+        for (int s = s0 + 2; s < s1 - 1; s += 2) term(s, (T)2, false);
+      }
 #pragma unroll
       for (int k = 0; k < W; ++k) bval[b][k] = (acc[k].value() * (blk.ds[b] / 3.0)) / QN;
     }

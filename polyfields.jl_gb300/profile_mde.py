@@ -5,8 +5,8 @@
 
 Default: one chain of `steps` RK2 contour steps through pf_propagate on an n^3 cubic grid
 (n x n plane kernels, n-point z pencils) with seeded fields.  --blend: `solves` density
-solves of the large-blend system (diblock + homopolymer, three chains advancing in the same
-launches, as in the benchmark) with Ns = `steps`.  Both keep the device footprint small
+solves of the large-blend system (diblock + homopolymer: three chains, one stream each, as in
+the benchmark) with Ns = `steps`.  Both keep the device footprint small
 (a few hundred MB at 128^3), so a profiler can replay each launch.
 """
 import argparse
