@@ -246,12 +246,12 @@ def run_gpu(args):
                 "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
                 "avg_step_us": mde_step_us}
-    # The step is issue bound before it is HBM bound: ncu counts 5.53e6 + 3.04e6 warp instructions
+    # The step is issue bound before it is HBM bound: ncu counts 5.59e6 + 3.02e6 warp instructions
     # for one chain step at 128^3 (plane + pencil pass); 152 SMs x 4 schedulers issue at most one
     # warp instruction per cycle each at the sampled SM clock.
     issue = None
     if n == 128:
-        winst = 5.53e6 + 3.04e6
+        winst = 5.59e6 + 3.02e6
         mhz = (clk or {}).get("sm_mhz") or 2070.0
         floor_us = winst / (152 * 4 * mhz * 1e6) * 1e6
         issue = {"warp_instructions_per_step": winst, "floor_us": floor_us, "frac": floor_us / mde_step_us}
