@@ -548,8 +548,11 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS) __maxnreg__((PlaneC
 
 
 
+// Two CTAs per SM for float planes.  Float64 instantiations take the registers of a whole SM:
+// a 128 x 65 half-spectrum plane (133 KB of shared memory) fits once per SM anyway, and a
+// two-CTA bound (56 registers) made the float64 transforms spill.
 template <typename T, int NX, int NY>
-__global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, PF_XY_MINB)
+__global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, sizeof(T) == 8 ? 1 : PF_XY_MINB)
     xy_step_kernel(const ChainJob<T>* __restrict__ jobs, int t, int nz, Twiddles<T> twg) {
   using C = PlaneCfg<NX, NY>;
   static_assert(NY > 1, "3D grids have Ny > 1");
