@@ -1911,6 +1911,9 @@ int guard(pf_system* h, F&& f) {
   } catch (const pf::PFError& e) {
     h->err = e.what();
     return e.code;
+  } catch (const pf::DeviceError& e) {
+    h->err = e.what();
+    return PF_ECUDA;
   } catch (const std::exception& e) {
     h->err = e.what();
     return PF_EARG;
@@ -1950,6 +1953,9 @@ int pf_system_create(pf_system** out, int nx, int ny, int nz, int precision) {
   } catch (const pf::PFError& e) {
     delete h;
     return e.code;
+  } catch (const std::exception&) {  // no exception crosses the C ABI
+    delete h;
+    return PF_ECUDA;
   }
   *out = h;
   return PF_OK;

@@ -1,8 +1,15 @@
 // Declarations shared by the kernel translation units and the host engine.
 #pragma once
 #include "pf_common.cuh"
+#include <stdexcept>
 
 namespace pf {
+
+// A CUDA call inside a kernel launcher failed (tensor-map encoding, launch configuration);
+// the C ABI reports it as PF_ECUDA.
+struct DeviceError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
 
 constexpr int kMaxParams = 6;   // triclinic cells have 6 parameters
 constexpr int kMaxMon = 8;      // monomer types per system

@@ -1190,7 +1190,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
 template <typename T>
 static void make_zmaps(CUtensorMap* km, CUtensorMap* lm, const Cx<T>* kbuf, const T* ld, int nkp, int nz) {
   auto enc = tmap_encoder();
-  if (!enc) throw std::runtime_error("cuTensorMapEncodeTiled is not available from the driver");
+  if (!enc) throw DeviceError("cuTensorMapEncodeTiled is not available from the driver");
   // box starts are multiples of 128 (scratch) and 64 (LD) bytes; rows must be 16-byte strided
   if (nkp % 4 != 0 || nz > 256 || (reinterpret_cast<uintptr_t>(kbuf) & 15) || (reinterpret_cast<uintptr_t>(ld) & 15))
     throw std::runtime_error("pencil pass: spectrum rows or buffers not 16-byte aligned");
@@ -1202,7 +1202,7 @@ static void make_zmaps(CUtensorMap* km, CUtensorMap* lm, const Cx<T>* kbuf, cons
     if (enc(km, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<Cx<T>*>(kbuf), dim, str, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      throw std::runtime_error("cuTensorMapEncodeTiled failed for a half-spectrum scratch");
+      throw DeviceError("cuTensorMapEncodeTiled failed for a half-spectrum scratch");
   }
   {
     const cuuint64_t dim[2] = {(cuuint64_t)nkp, (cuuint64_t)nz};
@@ -1211,7 +1211,7 @@ static void make_zmaps(CUtensorMap* km, CUtensorMap* lm, const Cx<T>* kbuf, cons
     if (enc(lm, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2,
             const_cast<T*>(ld), dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      throw std::runtime_error("cuTensorMapEncodeTiled failed for a bond operator");
+      throw DeviceError("cuTensorMapEncodeTiled failed for a bond operator");
   }
 }
 
@@ -1230,7 +1230,8 @@ static void launch_on(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sm
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
   cfg.numAttrs = pdl ? 1 : 0;
-  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+  if (e != cudaSuccess) throw DeviceError(std::string("kernel launch failed: ") + cudaGetErrorString(e));
 }
 
 // rounds (stages of tiles) per CTA of the pencil pipeline

@@ -104,6 +104,9 @@ int propagate_noalloc(int nx, int ny, int nz, T* hist, const T* lw, const T* ld,
   host.ld = ld_steps.data();
   try {
     launch_chains<T>(job_dev, 1, nsteps, GridDims{nx, ny, nz}, tw, st, &host);
+  } catch (const DeviceError& e) {
+    fprintf(stderr, "pf_propagate_noalloc: %s\n", e.what());
+    return E_CUDA;
   } catch (const std::exception& e) {
     fprintf(stderr, "pf_propagate_noalloc: %s\n", e.what());
     return E_ARG;
