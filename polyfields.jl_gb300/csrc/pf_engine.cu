@@ -466,6 +466,7 @@ struct System {
     // gram_p[a * nslot + b] = res(slot a) . res(slot b) for the slots of the window, gram_t
     // the current residual's products with the window (launch_gram_cached)
     DevBuf gram_p, gram_t;
+    DevBuf sum_hist;  // field + residual of each entry (the mix's single history once lam = 1)
     void reset() {
       exists = is_setup = false;
       nhist = 50;
@@ -478,6 +479,7 @@ struct System {
       field_hist.release();
       gram_p.release();
       gram_t.release();
+      sum_hist.release();
     }
   } and_;
   // EulerUpdater (kind 1, method 0 PEC / 1 PECE) and MomentumUpdater (kind 2, method 0 MOM,
@@ -1310,6 +1312,7 @@ struct System {
     const size_t slot = sizeof(double) * nmon() * ng;
     and_.res_hist.alloc(slot * (and_.nhist + 1));
     and_.field_hist.alloc(slot * (and_.nhist + 1));
+    and_.sum_hist.alloc(slot * (and_.nhist + 1));
     and_.gram_p.alloc(sizeof(double) * kMaxHist * kMaxHist);
     and_.gram_t.alloc(sizeof(double) * kMaxHist);
     PF_CU(cudaMemsetAsync(and_.res_hist.p, 0, and_.res_hist.bytes, st));
@@ -1399,6 +1402,7 @@ struct System {
     for (int j = 0; j <= ih; ++j) {
       h.res[j] = hist_slot(A.res_hist, j);
       h.field[j] = hist_slot(A.field_hist, j);
+      h.sum[j] = hist_slot(A.sum_hist, j);
     }
     // U and V from the current residual's products with the window and the cached pair
     // products of the older entries; every iteration (Euler warm-up included) adds its row, so
@@ -1407,6 +1411,7 @@ struct System {
     launch_gram_cached(h, res.as<double>(), ih, nall, A.gram_p.as<double>(), A.nhist + 1, A.base, part.as<double>(),
                        A.gram_t.as<double>(), packed.as<double>(), flag, st);
     if (it <= A.iter_euler) {
+      launch_add(h.sum[ih], h.field[ih], h.res[ih], nall, st);
       launch_axpy(w.as<double>(), res.as<double>(), A.lam_euler, nall, st);
     } else {
       launch_solve(packed.as<double>(), ih, cn.as<double>(), status.as<int>(), st);

@@ -675,7 +675,9 @@ void launch_solve(const double* packed, int ih, double* Cn, int* status, cudaStr
 // w = W + lam D,  W = w + sum_nn Cn[nn-1] (f[ih-nn] - f[ih]),  D = r + sum_nn Cn[nn-1] (r[ih-nn] - r).
 // Evaluated with the coefficients gathered, W = (w - C f[ih]) + sum c f[ih-nn] and
 // D = (1 - C) r + sum c r[ih-nn] (C = sum c): two FP64 FMAs per history entry and point instead
-// of two subtractions and two FMAs.
+// of two subtractions and two FMAs.  With lam = 1 (every iteration after the history has
+// filled) w = (w - C f[ih] + (1 - C) r) + sum c s[ih-nn] with s = f + r kept per entry: one
+// FMA and one history read per entry and point.  The pass also stores s[ih] = f[ih] + r.
 __global__ void mix_kernel(double* __restrict__ w, HistPtrs h, int ih, const double* __restrict__ Cn, double lam,
                            long n) {
   __shared__ double c[kMaxHist];
@@ -691,20 +693,44 @@ __global__ void mix_kernel(double* __restrict__ w, HistPtrs h, int ih, const dou
   const double C = csum, om = 1.0 - csum;
   const double* r = h.res[ih];
   const double* f = h.field[ih];
+  double* s = h.sum[ih];
+  if (lam == 1.0) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+      const double fi = f[i], ri = r[i];
+      double acc = fma(om, ri, fma(-C, fi, w[i]));
+      for (int nn = 1; nn <= ih; ++nn) acc = fma(c[nn - 1], h.sum[ih - nn][i], acc);
+      s[i] = fi + ri;
+      w[i] = acc;
+    }
+    return;
+  }
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    double W = fma(-C, f[i], w[i]), D = om * r[i];
+    const double fi = f[i], ri = r[i];
+    double W = fma(-C, fi, w[i]), D = om * ri;
     for (int nn = 1; nn <= ih; ++nn) {
       W = fma(c[nn - 1], h.field[ih - nn][i], W);
       D = fma(c[nn - 1], h.res[ih - nn][i], D);
     }
+    s[i] = fi + ri;
     w[i] = fma(lam, D, W);
   }
 }
-
 void launch_mix(double* w, const HistPtrs& h, int ih, const double* Cn, double lam, long n_all, cudaStream_t st) {
   int nb = (int)((n_all + 255) / 256);
   if (nb > 8192) nb = 8192;
   mix_kernel<<<nb, 256, 0, st>>>(w, h, ih, Cn, lam, n_all);
+  count_launches(1);
+}
+
+__global__ void add_kernel(double* __restrict__ out, const double* __restrict__ a, const double* __restrict__ b,
+                           long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    out[i] = a[i] + b[i];
+}
+void launch_add(double* out, const double* a, const double* b, long n, cudaStream_t st) {
+  int nb = (int)((n + 255) / 256);
+  if (nb > 8192) nb = 8192;
+  add_kernel<<<nb, 256, 0, st>>>(out, a, b, n);
   count_launches(1);
 }
 

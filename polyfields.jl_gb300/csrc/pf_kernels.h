@@ -226,6 +226,7 @@ void launch_axpy(double* y, const double* x, double a, long n, cudaStream_t st);
 struct HistPtrs {
   const double* res[kMaxHist];    // logical order 0..ih
   const double* field[kMaxHist];
+  double* sum[kMaxHist];          // field + residual of each entry (entry ih written by the step)
 };
 void launch_gram(const HistPtrs& h, int ih, long n_all, double* part, double* out, cudaStream_t st);
 // The packed U, V of launch_gram from the cached history products P (nslot x nslot, physical
@@ -234,5 +235,7 @@ void launch_gram_cached(const HistPtrs& h, const double* r, int ih, long n_all, 
                         double* part, double* t, double* packed, int* flag, cudaStream_t st);
 void launch_solve(const double* packed, int ih, double* Cn, int* status, cudaStream_t st);
 void launch_mix(double* w, const HistPtrs& h, int ih, const double* Cn, double lam, long n_all, cudaStream_t st);
+// out = a + b (the history sum of an entry in iterations without a mix)
+void launch_add(double* out, const double* a, const double* b, long n, cudaStream_t st);
 
 }  // namespace pf
