@@ -140,7 +140,7 @@ def cpu_baseline_sample(min_seconds=10.0):
 
 def run_reference(args):
     """Reference arm: the FP64 CPU restatement of the reference's path (the oracle); each step
-    is a bounded sample (20 contour steps of the 128^3 propagator) scaled to iterations/s."""
+    is a bounded sample (100 contour steps of the 128^3 propagator) scaled to iterations/s."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
