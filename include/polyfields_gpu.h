@@ -88,6 +88,10 @@ int pf_get_precision(const pf_system* sys, int* precision);
  * 0 = RK2 operator splitting, 1 = RQM4 Richardson extrapolation of one full and two half RK2
  * steps (mde.jl:83-104; float64 chains only: PF_EUNSUPPORTED with PF_FP32). */
 int pf_set_mde(pf_system* sys, int method);
+/* SCFTOptions.savepath (src/simulate.jl:12-19): with nsave > 0 in the options, pf_scft writes
+ * the fields to this file every nsave steps (simulate.jl:124-128) in savefields' JSON layout
+ * (src/fileio.jl:77-97).  NULL or "" disables it. */
+int pf_set_savepath(pf_system* sys, const char* path);
 
 /* UnitCell(dim, crystal, params) + add_cell!  (src/system/cell.jl:31-52, system.jl:102-106).
  * crystal is the reference's Symbol name without ':' ("lamellar", "hexagonal", "cubic", ...). */

@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <array>
 #include <chrono>
+#include <ctime>
 
 #include "pf_kernels.h"
 #include "polyfields_gpu.h"
@@ -443,6 +444,7 @@ struct System {
   bool jobs_dirty[2] = {true, true};
   bool timing = false;
   int mde = 0;     // 0 RK2 (mde.jl:65-81), 1 RQM4 (mde.jl:83-104, float64 chains)
+  std::string savepath;  // SCFTOptions.savepath (simulate.jl:12-19), written every nsave steps
   int adj_ckpt = 0;  // pullback: 0 = read the stored histories, K > 0 = recompute between checkpoints
   int ensemble = 0;  // 0 Canonical, 1 Grand (system.jl:6-13)
   DevBuf one;        // a device 1.0 (grand-canonical densities are not divided by Q)
@@ -1770,6 +1772,44 @@ struct System {
     return fc && sc;
   }
 
+  // savefields(sys, path) (fileio.jl:77-97) for the omega fields: dim, grid, mids, date,
+  // crystal, cell_params, field_type and the fields as nested [z][y][x] lists, one per monomer id.
+  void save_fields(const std::string& path) {
+    std::vector<double> h((size_t)ng * nmon());
+    PF_CU(cudaMemcpyAsync(h.data(), w.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
+    PF_CU(cudaStreamSynchronize(st));
+    FILE* f = fopen(path.c_str(), "w");
+    if (!f) throw PFError(E_ARG, "cannot open " + path + " for writing");
+    char date[32] = "";
+    const std::time_t now = std::time(nullptr);
+    std::tm tmv{};
+    if (localtime_r(&now, &tmv)) std::strftime(date, sizeof date, "%Y-%m-%d %H:%M:%S", &tmv);
+    fprintf(f, "{\n    \"dim\": %d,\n    \"grid\": [%d, %d, %d],\n    \"mids\": [", cell.dim, nx, ny, nz);
+    for (int a = 0; a < nmon(); ++a) fprintf(f, "%s%d", a ? ", " : "", mon_ids[a]);
+    fprintf(f, "],\n    \"date\": \"%s\",\n    \"crystal\": \"%s\",\n    \"cell_params\": [", date,
+            cell.crystal.c_str());
+    for (int i = 0; i < cell.np(); ++i) fprintf(f, "%s%.17g", i ? ", " : "", cell.params[i]);
+    fprintf(f, "],\n    \"field_type\": \"omega\",\n    \"fields\": {");
+    for (int a = 0; a < nmon(); ++a) {
+      fprintf(f, "%s\n        \"%d\": [", a ? "," : "", mon_ids[a]);
+      const double* g = h.data() + (size_t)a * ng;
+      for (int z = 0; z < nz; ++z) {
+        fprintf(f, "%s[", z ? ", " : "");
+        for (int y = 0; y < ny; ++y) {
+          fprintf(f, "%s[", y ? ", " : "");
+          const double* row = g + ((size_t)z * ny + y) * nx;
+          for (int x = 0; x < nx; ++x) fprintf(f, "%s%.17g", x ? ", " : "", row[x]);
+          fprintf(f, "]");
+        }
+        fprintf(f, "]");
+      }
+      fprintf(f, "]");
+    }
+    fprintf(f, "\n    }\n}\n");
+    const bool bad = ferror(f) != 0;
+    if (fclose(f) != 0 || bad) throw PFError(E_ARG, "writing " + path + " failed");
+  }
+
   pf_scft_results scft(const pf_scft_options& o, bool vcell) {
     auto t0 = std::chrono::steady_clock::now();
     pf_scft_results r{};
@@ -1819,6 +1859,7 @@ struct System {
         if (o.nsout > 0) printf("Converged @ step = %d: ferr = %8e, fhelm = %.5e\n", step, ferr, fhelm);
         break;
       }
+      if (o.nsave > 0 && step % o.nsave == 0 && !savepath.empty()) save_fields(savepath);  // simulate.jl:124-128
       if (mixed && prec == 1) {
         if (ferr < 0.99 * best) {
           best = ferr;
@@ -1997,6 +2038,10 @@ int pf_set_ensemble(pf_system* sys, int ensemble) {
 
 int pf_set_edwards(pf_system* sys, int mid, double u) {
   return guard(sys, [&](pf::System& s) { s.set_edwards(mid, u); });
+}
+
+int pf_set_savepath(pf_system* sys, const char* path) {
+  return guard(sys, [&](pf::System& s) { s.savepath = path ? std::string(path) : std::string(); });
 }
 
 int pf_set_mde(pf_system* sys, int method) {

@@ -5,7 +5,8 @@ of include/polyfields_gpu.h); this package mirrors the reference's public API on
 """
 from .api import (AndersonUpdater, Canonical, Diblock, DomainUpdater, EdwardsInteraction, EulerUpdater, FieldSystem, FloryInteraction, FP32, FP64,
                   Grand, Homopolymer, MomentumUpdater, Monomer, Multiblock, Point, SCFTOptions, SCFTResults, UnitCell, add_interaction,
-                  add_species, chain_grid, density, field_error, fieldinit, free_energy, free_energy_bulk, loadfields,
+                  add_species, chain_grid, density, field_error, fieldinit, free_energy, free_energy_bulk, interpolate_grid,
+                  loadfields,
                   residuals, savefields, scfstress, scft, scft_batch, set_interaction, setup, step,
                   updater_with_system, validate)
 from ._lib import LIB_PATH, PolyFieldsError, load as load_library

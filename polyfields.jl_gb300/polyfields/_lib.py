@@ -68,6 +68,7 @@ SIGNATURES = {
     "pf_domain_stress_error": (_c_int, [_vp, _dptr]),
     "pf_scft": (_c_int, [_vp, ctypes.POINTER(ScftOptions), _c_int, ctypes.POINTER(ScftResults)]),
     "pf_set_mde": (_c_int, [_vp, _c_int]),
+    "pf_set_savepath": (_c_int, [_vp, ctypes.c_char_p]),
     "pf_set_edwards": (_c_int, [_vp, _c_int, ctypes.c_double]),
     "pf_set_ensemble": (_c_int, [_vp, _c_int]),
     "pf_euler_create": (_c_int, [_vp, _c_int, ctypes.c_double]),

@@ -10,6 +10,8 @@ from __future__ import annotations
 
 import ctypes
 import json
+import os
+import warnings
 import math
 from dataclasses import dataclass, field as dc_field
 from typing import Dict, List, Optional, Sequence
@@ -635,9 +637,9 @@ def scft(sys: FieldSystem, updater: AndersonUpdater, domain: Optional[DomainUpda
         domain._bind(sys)
     o = L.ScftOptions(opts.nsteps, opts.nsout, opts.nsave, 0, opts.ftol, opts.stol, opts.mixed_switch_ferr)
     r = L.ScftResults()
-    L.check(L.load().pf_scft(sys._h, ctypes.byref(o), 1 if domain is not None else 0, ctypes.byref(r)), sys._h)
-    if opts.savepath:
-        savefields(sys, opts.savepath)
+    lib = L.load()
+    L.check(lib.pf_set_savepath(sys._h, (opts.savepath or "").encode()), sys._h)
+    L.check(lib.pf_scft(sys._h, ctypes.byref(o), 1 if domain is not None else 0, ctypes.byref(r)), sys._h)
     return SCFTResults(r.time, r.nsteps, bool(r.converged), r.ferr, r.serr, r.fhelm, r.switch_step)
 
 
@@ -683,17 +685,131 @@ def scft_batch(systems: Sequence[FieldSystem], updaters: Sequence[AndersonUpdate
 # =============================================================================
 # Field initialisation and IO (src/fileio.jl)
 # =============================================================================
-def fieldinit(sys: FieldSystem, fields: Optional[Dict[int, np.ndarray]] = None, *, seed: int = -1,
-              scale: float = 0.1) -> None:
-    """fieldinit!(sys, fields::Dict) (fileio.jl:25-54) or, without ``fields``,
-    fieldinit!(sys; seed, scale) (fileio.jl:14-23) with NumPy's PCG64 normal stream in place
-    of Julia's MersenneTwister randn."""
+def _natural_spline_along(a: np.ndarray, axis: int, pos: np.ndarray) -> np.ndarray:
+    """Interpolating natural cubic spline (second derivative 0 at both ends) through the samples
+    of ``a`` at integer positions 0..n-1 along ``axis``, evaluated at the real positions ``pos``."""
+    a = np.moveaxis(np.asarray(a, dtype=np.float64), axis, 0)
+    n = a.shape[0]
+    flat = a.reshape(n, -1)
+    m = np.zeros_like(flat)  # second derivatives at the knots
+    if n > 2:
+        # (m[i-1] + 4 m[i] + m[i+1]) = 6 (y[i-1] - 2 y[i] + y[i+1]),  m[0] = m[n-1] = 0 (Thomas)
+        rhs = 6.0 * (flat[:-2] - 2.0 * flat[1:-1] + flat[2:])
+        k = n - 2
+        c = np.zeros(k)
+        d = np.zeros_like(rhs)
+        c[0] = 1.0 / 4.0
+        d[0] = rhs[0] / 4.0
+        for i in range(1, k):
+            den = 4.0 - c[i - 1]
+            c[i] = 1.0 / den
+            d[i] = (rhs[i] - d[i - 1]) / den
+        x = np.zeros_like(rhs)
+        x[-1] = d[-1]
+        for i in range(k - 2, -1, -1):
+            x[i] = d[i] - c[i] * x[i + 1]
+        m[1:-1] = x
+    j = np.clip(np.floor(pos).astype(int), 0, max(n - 2, 0))
+    t = (pos - j)[:, None]
+    if n == 1:
+        out = np.repeat(flat[:1], len(pos), axis=0)
+    else:
+        y0, y1, m0, m1 = flat[j], flat[j + 1], m[j], m[j + 1]
+        out = (1 - t) * y0 + t * y1 + ((1 - t) ** 3 - (1 - t)) * m0 / 6.0 + (t ** 3 - t) * m1 / 6.0
+    return np.moveaxis(out.reshape((len(pos),) + a.shape[1:]), 0, axis)
+
+
+def interpolate_grid(grid: np.ndarray, dims) -> np.ndarray:
+    """interpolate_grid(grid, outshape) (src/utils.jl:64-109): a field or density grid of shape
+    (Nz, Ny, Nx) resampled to ``dims`` = (Nx', Ny', Nz') by the cubic B-spline with linear ("Line",
+    zero second derivative) boundaries that the reference builds with Interpolations.jl
+    (BSpline(Cubic(Line(OnGrid())))): on the grid points that is the interpolating natural cubic
+    spline, applied axis by axis (the tensor-product spline factorises).  As in the reference the
+    output points run from the first to the last input point (range(1, n_in; length = n_out)); an
+    axis of length 1 in the input is copied along the output axis, an output axis of length 1
+    takes the first input point."""
+    grid = np.asarray(grid, dtype=np.float64)
+    if grid.ndim != 3:
+        raise ValueError("grid must be a 3-D array of shape (Nz, Ny, Nx)")
+    out_shape = (int(dims[2]), int(dims[1]), int(dims[0]))
+    in_single = tuple(i for i in range(3) if grid.shape[i] == 1)
+    out_single = tuple(i for i in range(3) if out_shape[i] == 1)
+    if in_single != out_single:
+        warnings.warn("Interpolating to different dimensions -- output array may be inaccurate.")
+    a = grid
+    for axis in range(3):
+        nin, nout = a.shape[axis], out_shape[axis]
+        if nin == nout:
+            continue
+        if nin == 1:
+            a = np.repeat(a, nout, axis=axis)
+        elif nout == 1:
+            a = np.take(a, [0], axis=axis)
+        else:
+            a = _natural_spline_along(a, axis, np.linspace(0.0, nin - 1.0, nout))
+    return np.ascontiguousarray(a)
+
+
+def _potentials_from(sys: FieldSystem, rho: Dict[int, np.ndarray]) -> Dict[int, np.ndarray]:
+    """potentials!(sys) (system.jl:296-310) from given densities: Flory (flory.jl:82-100)
+    pot_a += chi_ab rho_b / v_b and Edwards (edwards.jl) pot_a += u_a rho_a / v_a."""
+    pots = {mid: np.zeros(sys.shape) for mid in sys.monomers}
+    for itx in sys.interactions:
+        if isinstance(itx, FloryInteraction):
+            for (a, b), chi in itx.chis.items():
+                if a in pots and b in rho:
+                    pots[a] += chi * (rho[b] / sys.monomers[b].vol)
+                if b in pots and a in rho:
+                    pots[b] += chi * (rho[a] / sys.monomers[a].vol)
+        elif isinstance(itx, EdwardsInteraction):
+            for mid, u in itx.uvals.items():
+                if mid in pots and mid in rho:
+                    pots[mid] += u * (rho[mid] / sys.monomers[mid].vol)
+    return pots
+
+
+def fieldinit(sys: FieldSystem, fields=None, *, field_type: str = "omega", interpolate: bool = True,
+              load_cell: bool = True, seed: int = -1, scale: float = 0.1) -> None:
+    """fieldinit!(sys, fields::Dict; field_type, interpolate) (fileio.jl:25-54),
+    fieldinit!(sys, path; load_cell, interpolate) (fileio.jl:56-64) when ``fields`` is a path to
+    a savefields JSON, or, without ``fields``, fieldinit!(sys; seed, scale) (fileio.jl:14-23)
+    with NumPy's PCG64 normal stream in place of Julia's MersenneTwister randn.
+
+    Grids of another shape are resampled with interpolate_grid (or rejected with
+    interpolate=False).  field_type "rho" takes densities: the fields become their potentials,
+    mean-subtracted in the canonical ensemble (uniform_fields!, system.jl:348-357)."""
+    if isinstance(fields, (str, os.PathLike)):
+        data = loadfields(str(fields))
+        if load_cell:
+            sys.add_cell(UnitCell(data["dim"], data["crystal"], *data["cell_params"]))
+        fieldinit(sys, data["fields"], field_type=data["field_type"], interpolate=interpolate)
+        return
     if fields is None:
         rng = np.random.Generator(np.random.PCG64(seed if seed >= 0 else None))
         fields = {mid: scale * rng.standard_normal(sys.shape) for mid in sorted(sys.monomers)}
+    ftype = str(field_type).lstrip(":")
+    if ftype not in ("omega", "rho"):
+        raise ValueError(f"unknown field_type {field_type}")
+    given: Dict[int, np.ndarray] = {}
     for mid, arr in fields.items():
-        if mid in sys.monomers:
+        mid = int(mid)
+        if mid not in sys.monomers:
+            warnings.warn(f"Monomer with ID = {mid} not present in system -- skipping.")
+            continue
+        arr = np.asarray(arr, dtype=np.float64)
+        if arr.shape != sys.shape:
+            if not interpolate:
+                raise ValueError(f"Input field dimensions {arr.shape[::-1]} does not match system grid {sys.dims}.")
+            arr = interpolate_grid(arr, sys.dims)
+        given[mid] = arr
+    if ftype == "omega":
+        for mid, arr in given.items():
             sys.fields[mid] = arr
+    else:
+        rho = {mid: sys.density[mid] for mid in sys.monomers}
+        rho.update(given)
+        for mid, pot in _potentials_from(sys, rho).items():
+            sys.fields[mid] = pot - np.mean(pot) if sys.ensemble == Canonical else pot
     sys.residuals_update()
 
 
