@@ -4,8 +4,8 @@ The compute path is libpolyfields_gpu.so (hand-written sm_103a CUDA kernels behi
 of include/polyfields_gpu.h); this package mirrors the reference's public API on top of it.
 """
 from .api import (AndersonUpdater, Canonical, Diblock, DomainUpdater, EdwardsInteraction, EulerUpdater, FieldSystem, FloryInteraction, FP32, FP64,
-                  Grand, Homopolymer, MomentumUpdater, Monomer, Multiblock, Point, SCFTOptions, SCFTResults, UnitCell, add_interaction,
-                  add_species, chain_grid, density, field_error, fieldinit, free_energy, free_energy_bulk, interpolate_grid,
+                  Grand, Homopolymer, MomentumUpdater, Monomer, Multiblock, Point, SCFTOptions, SCFTResults, UnitCell, add_cell,
+                  add_interaction, add_monomer, add_species, chain_grid, monomer_fraction, uniform_fields, density, field_error, fieldinit, free_energy, free_energy_bulk, interpolate_grid,
                   loadfields,
                   residuals, savefields, scfstress, scft, scft_batch, set_interaction, setup, step,
                   updater_with_system, validate)

@@ -435,8 +435,31 @@ class FieldSystem:
         L.check(L.load().pf_synchronize(self._h), self._h)
 
 
+def add_monomer(sys: FieldSystem, mon: Monomer) -> None:
+    """add_monomer!(sys, mon) (system.jl:113-135)."""
+    sys.add_monomer(mon)
+
+
+def add_cell(sys: FieldSystem, cell: UnitCell) -> None:
+    """add_cell!(sys, cell) (system.jl:102-111)."""
+    sys.add_cell(cell)
+
+
 def add_species(sys: FieldSystem, species, val: float) -> None:
     sys.add_species(species, val)
+
+
+def monomer_fraction(species, mid: int) -> float:
+    """monomer_fraction(species, mid) (multiblock.jl:93-102, point.jl)."""
+    return species.monomer_fraction(int(mid))
+
+
+def uniform_fields(sys: FieldSystem) -> None:
+    """uniform_fields!(sys) (system.jl:348-357): every field becomes the potential of the current
+    densities, mean-subtracted in the canonical ensemble."""
+    rho = {mid: sys.density[mid] for mid in sys.monomers}
+    for mid, pot in _potentials_from(sys, rho).items():
+        sys.fields[mid] = pot - np.mean(pot) if sys.ensemble == Canonical else pot
 
 
 def add_interaction(sys: FieldSystem, itx) -> None:

@@ -78,3 +78,11 @@ def test_potentials_from_densities_restate_flory_and_edwards():
     pots = api._potentials_from(s, rho)
     assert np.allclose(pots[1], 0.3 * 0.6 / 2.0)
     assert np.allclose(pots[2], 0.3 * 0.4 / 1.0 + 5.0 * 0.6 / 2.0)
+
+
+def test_monomer_fraction_free_function_matches_species():
+    A, B = pf.Monomer(1), pf.Monomer(2)
+    chain = pf.Diblock(A, B, 100, 0.3, 1.0, 1.0, 100)
+    assert pf.monomer_fraction(chain, 1) == pytest.approx(0.3)
+    assert pf.monomer_fraction(chain, 2) == pytest.approx(0.7)
+    assert pf.monomer_fraction(chain, 3) == 0.0
