@@ -436,12 +436,12 @@ class FieldSystem:
 
 
 def add_monomer(sys: FieldSystem, mon: Monomer) -> None:
-    """add_monomer!(sys, mon) (system.jl:113-135)."""
+    """add_monomer!(sys, mon) (system.jl:113-128)."""
     sys.add_monomer(mon)
 
 
 def add_cell(sys: FieldSystem, cell: UnitCell) -> None:
-    """add_cell!(sys, cell) (system.jl:102-111)."""
+    """add_cell!(sys, cell) (system.jl:102-106)."""
     sys.add_cell(cell)
 
 
