@@ -72,3 +72,14 @@ def test_scft_nsave_writes_the_fields(tmp_path):
     q = tmp_path / "never.json"
     pf.scft(g, pf.AndersonUpdater(nhist=5), opts=pf.SCFTOptions(nsteps=2, nsave=0, ftol=1e-14, savepath=str(q)))
     assert not q.exists()
+
+
+def test_uniform_fields_matches_oracle():
+    """uniform_fields!(sys) (system.jl:348-357) on the current densities."""
+    kw = dict(dims=(32, 32, 1), crystal="hexagonal", params=(9.0,), f=0.3, chi=0.3)
+    o = SY.diblock_system(O, **kw)
+    g = SY.diblock_system(pf, precision="fp64", **kw)
+    o.uniform_fields()
+    pf.uniform_fields(g)
+    for mid in (1, 2):
+        assert rel(g.fields[mid], o.fields[mid]) < 1e-10
