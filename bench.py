@@ -11,6 +11,9 @@ FP64 propagator rate is measured after it on the same state.
 
   python bench.py [--steps K] [--warmup W]            # GPU engine (one JSON line)
   python bench.py --impl reference [--steps K ...]    # the FP64 CPU restatement (oracle)
+  python bench.py --mode tts [--size N] [--seeds S]   # time to solution: mixed vs plain FP64
+  python bench.py --mode sweep [--count 256]          # batched 2D hexagonal phase-diagram sweep
+  python bench.py --mode profile [--size N] [--ns NS] # a few density solves, small, for ncu
 
 Inputs are synthetic (seeded NumPy PCG64 fields of the benchmark's shapes) and the working
 set (propagator histories, ~5 GB) is far larger than the 129 MB L2.
@@ -196,6 +199,9 @@ def run_gpu(args):
     n = args.size
     sysm = blend3d_system(pf, n=n, precision="fp32")
     ng = n ** 3
+    # the initial state's free energy: tests/test_gpu_parity_large.py checks this state (both
+    # precisions) against the FP64 oracle
+    fhelm_initial = sysm.free_energy()
     upd = pf.AndersonUpdater(nhist=NHIST)
     upd.setup(sysm)
     sysm.set_timing(True)
@@ -294,16 +300,116 @@ def run_gpu(args):
                 "mde_step_us": 1000.0 * a64 / nmde}
 
     cpu = cpu_baseline_sample(args.cpu_seconds) if args.cpu_seconds > 0 else None
+    del upd, sysm
+    # time to solution, mixed vs plain FP64, on a grid that fits the run's time (median of seeds)
+    tts = tts_summary(args.tts_size, [12345 + 1000 * i for i in range(args.seeds)]) if args.tts_size > 0 else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 propagators + f64 reductions", "data": "synthetic", "config": dict(WORKLOAD, size=n),
             "mde_steps_per_s": value * nmde, "mde_steps_per_iter": nmde, "propagate_ms_per_iter": prop_step_ms,
             "density_ms_per_iter": dens_ms / args.steps, "host_ms_per_step": 1000.0 * t_host / args.steps,
             "fp64": fp64, "mixed_vs_fp64_iter_speedup": (value / fp64["iters_per_s"]) if fp64 else None,
-            "ferr": ferr, "fhelm": fhelm, "roofline": roofline, "issue_roofline": issue, "e2e": e2e,
+            "ferr": ferr, "fhelm": fhelm, "fhelm_initial": fhelm_initial, "roofline": roofline, "issue_roofline": issue, "e2e": e2e,
             "gpu_launches": int(launches),
-            "clocks": clk, "cpu_baseline": cpu}
+            "clocks": clk, "cpu_baseline": cpu, "time_to_solution": tts}
     print(json.dumps(line))
+    return 0
+
+
+def tts_pair(n, seed, ftol=1e-8, nsteps=4000, switch=3e-6, nhist=NHIST):
+    """Time to solution of the large blend on an n^3 grid (cell held at L0 = 14, seeded start):
+    scft! with float64 propagators throughout, and the mixed path (float32 propagators until
+    ferr < switch, then float64 polish), both to ftol.  Wall time of each pf_scft call."""
+    import polyfields as pf
+    from polyfields import workloads as W
+    out = {}
+    for mode in ("fp64", "mixed"):
+        sysm = W.blend3d_system(pf, n=n, precision="fp64" if mode == "fp64" else "fp32", seed=seed)
+        sysm.synchronize()
+        opts = pf.SCFTOptions(nsteps=nsteps, ftol=ftol, mixed_switch_ferr=switch if mode == "mixed" else 0.0)
+        t0 = time.perf_counter()
+        r = pf.scft(sysm, pf.AndersonUpdater(nhist=nhist), opts=opts)
+        sysm.synchronize()
+        out[mode] = {"wall_s": time.perf_counter() - t0, "iterations": r.nsteps, "converged": bool(r.converged),
+                     "switch_step": r.switch_step, "ferr": r.ferr, "fhelm": r.fhelm}
+        del sysm
+    out["wall_ratio"] = out["fp64"]["wall_s"] / out["mixed"]["wall_s"]
+    out["abs_dfhelm"] = abs(out["mixed"]["fhelm"] - out["fp64"]["fhelm"])
+    return out
+
+
+def tts_summary(n, seeds):
+    runs = [dict(seed=sd, **tts_pair(n, sd)) for sd in seeds]
+    ratios = sorted(r["wall_ratio"] for r in runs)
+    return {"workload": f"large blend {n}^3 (cell held at L0 = 14), Anderson nhist {NHIST}, ftol 1e-8; mixed = "
+                        f"float32 propagators to ferr 3e-6, then float64 polish",
+            "seeds": list(seeds), "wall_ratio_median": statistics.median(ratios),
+            "wall_ratio_min": ratios[0], "wall_ratio_max": ratios[-1],
+            "abs_dfhelm_max": max(r["abs_dfhelm"] for r in runs),
+            "all_converged": all(r["fp64"]["converged"] and r["mixed"]["converged"] for r in runs), "runs": runs}
+
+
+def run_tts(args):
+    """Time to solution, mixed vs plain FP64, over several seeds (median and spread)."""
+    seeds = [12345 + 1000 * i for i in range(args.seeds)]
+    line = {"mode": "tts", "metric": "wall-time ratio FP64 / mixed to ftol 1e-8 (|dfhelm| <= 1e-8)",
+            "unit": "x", "higher_is_better": True}
+    line.update(tts_summary(args.size, seeds))
+    line["value"] = line["wall_ratio_median"]
+    print(json.dumps(line))
+    return 0
+
+
+def run_profile(args):
+    """A small device footprint for profilers: `solves` density solves of the large blend on an
+    n^3 grid with Ns = args.ns contour steps per chain (three chains, one stream each, as in the
+    benchmark), so that ncu can replay every launch."""
+    import polyfields as pf
+    from polyfields import workloads as W
+    sysm = W.blend3d_system(pf, n=args.size, precision=args.precision, Ns=args.ns)
+    for _ in range(args.solves):
+        sysm.density_update()
+    sysm.synchronize()
+    print(json.dumps({"mode": "profile", "grid": args.size, "Ns": args.ns, "solves": args.solves,
+                      "precision": args.precision, "Q": [sp.Q for sp in sysm.species]}))
+    return 0
+
+
+def run_sweep(args):
+    """Batched phase-diagram sweep of 2D hexagonal diblock instances (grids 32^2 .. 128^2, chiN ~
+    U[12, 30], fA ~ U[0.25, 0.5], a0 ~ U[4, 9], Ns 100, seeded noise plus six-fold cosines; one
+    seeded parameter stream): scft! with AndersonUpdater(nhist = 10), cells held fixed
+    (--sweep-domain: DomainUpdater(nskip = 5, nper = 20)), float32 until ferr < 1e-5 then
+    float64 polish to ftol = 1e-7 (--precision fp32) or float64 throughout.  Under torchrun the
+    instances are sharded over the ranks by cost and gathered on rank 0."""
+    from polyfields import sweep as S
+    from polyfields import workloads as W
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("gloo")
+    params = W.hex_sweep_params(args.count, 12345)
+    t0 = time.perf_counter()
+    res = S.run_sharded(params, rank, world, precision=args.precision, nsteps=3000, nthreads=args.nthreads,
+                        vcell=args.sweep_domain)
+    wall = time.perf_counter() - t0
+    if rank == 0:
+        iters = sum(r["iterations"] for r in res)
+        print(json.dumps({
+            "mode": "sweep", "metric": "instances/s", "value": args.count / wall, "unit": "instances/s",
+            "workload": f"{args.count} hexagonal diblock instances, grids 32^2..128^2, Ns 100, nhist 10, "
+                        + ("nskip 5 nper 20, ftol=stol=1e-7" if args.sweep_domain else "fixed cells, ftol=1e-7"),
+            "precision": "fp32 then fp64 polish" if args.precision == "fp32" else "fp64",
+            "n_ranks": world, "nthreads": args.nthreads, "wall_s": wall, "scft_iters_total": iters,
+            "scft_iters_per_s": iters / wall, "converged": sum(1 for r in res if r["converged"]),
+            "failed": sum(1 for r in res if r["status"] != 0),
+            "errors": sorted({r["error"] for r in res if r["status"] != 0})[:4]}))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
     return 0
 
 
@@ -316,9 +422,25 @@ def main():
     ap.add_argument("--size", type=int, default=N_GRID, help="grid points per axis (default 128)")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="length of the CPU baseline sample (0: skip)")
+    ap.add_argument("--mode", default="iter", choices=["iter", "tts", "sweep", "profile"])
+    ap.add_argument("--seeds", type=int, default=3, help="tts: seeds of the time-to-solution runs")
+    ap.add_argument("--tts-size", type=int, default=64,
+                    help="iter: grid of the time-to-solution leg (0: skip); tts mode uses --size")
+    ap.add_argument("--precision", default="fp32", help="profile / sweep: fp32 (mixed) or fp64")
+    ap.add_argument("--ns", type=int, default=20, help="profile: contour steps per chain")
+    ap.add_argument("--solves", type=int, default=3, help="profile: density solves")
+    ap.add_argument("--count", type=int, default=256, help="sweep: instances")
+    ap.add_argument("--nthreads", type=int, default=32, help="sweep: host threads")
+    ap.add_argument("--sweep-domain", action="store_true", help="sweep: variable cells (DomainUpdater)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "profile":
+        return run_profile(args)
+    if args.mode == "sweep":
+        return run_sweep(args)
+    if args.mode == "tts":
+        return run_tts(args)
     return run_gpu(args)
 
 

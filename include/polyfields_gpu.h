@@ -4,8 +4,8 @@
  *
  * The reference is pure Julia with no C interface; each entry point below replaces the Julia
  * function cited beside it (file:line within the PolyFields.jl project).  A Julia binding
- * calls these through `ccall`; the Python package in
- * polyfields.jl_gb300/polyfields calls them through ctypes.
+ * calls these through `ccall` (polyfields.jl_gb300/julia/PolyFieldsGPU.jl); the Python package
+ * in polyfields.jl_gb300/polyfields calls them through ctypes.
  *
  * Conventions
  *  - Every function returns an int status (PF_OK = 0).  On failure the handle's
@@ -30,7 +30,8 @@ enum pf_status {
   PF_ECUDA = 2,       /* CUDA runtime failure */
   PF_ENAN = 3,        /* "Diverging field updater -- breaking." (src/simulate.jl:109-111) */
   PF_ESINGULAR = 4,   /* "Error inverting Umn matrix" (src/updaters/anderson.jl:184-189) */
-  PF_ETIMEOUT = 5,    /* a bounded device wait gave up */
+  PF_ETIMEOUT = 5,    /* a bounded device wait gave up (a 3D pencil pass's wait for a TMA copy); the
+                         results of that solve are invalid, the handle stays usable */
   PF_ESTATE = 6,      /* call out of order (e.g. step before setup) */
   PF_ENOMEM = 7,      /* device allocation failed */
   PF_EUNSUPPORTED = 8, /* grid length outside the supported FFT sizes */
@@ -225,9 +226,22 @@ int pf_propagate(pf_system* sys, const double* omega, double vol, double b, doub
  * the process exits): the 3D half spectrum must fit 16 MiB - 96 KiB (float32 up to 128^3,
  * float64 up to 96^3), otherwise PF_ETOOLARGE; nsteps <= 3840.  Calls whose GPU work
  * overlaps race on that array.  The first call on each device looks up the array's device
- * address, so make it before any stream capture. */
+ * address, so make it before any stream capture.  A 3D call whose pencil pass gave up waiting
+ * for a TMA copy leaves a status word set in the array: pf_propagate_noalloc_status reports it. */
 int pf_propagate_noalloc(int nx, int ny, int nz, int precision, void* hist, const void* lw, const void* ld,
                          int nsteps, void* stream);
+/* Status of the pf_propagate_noalloc calls made since the last query on this device: waits for
+ * `stream` (queue it after the calls' work), then returns PF_ETIMEOUT when a pencil pass of one
+ * of them gave up waiting for a TMA copy (their output is invalid) and PF_OK otherwise, and
+ * clears the word.  Allocates nothing. */
+int pf_propagate_noalloc_status(void* stream);
+
+/* Time limit of the bounded waits of this handle's 3D pencil passes for their TMA copies
+ * (default 1 s of GPU time; [0, 10]).  A wait that runs out marks the solve invalid: the next
+ * call that reads results returns PF_ETIMEOUT and the handle stays usable.  0 makes every such
+ * wait give up at once, which exercises that path in tests without a fault; copies already in
+ * flight are still drained with the default limit before a pencil pass exits. */
+int pf_set_wait_limit(pf_system* sys, double seconds);
 
 /* ---- measurement ---- */
 /* Device time (ms) of the last density solve's propagator launches, measured with CUDA

@@ -417,6 +417,10 @@ struct System {
   DevBuf w, pot, res, rho;   // nmon * ng doubles
   DevBuf rbar, wbar;         // adjoint: dL/drho (set by the caller) and dL/dw, nmon * ng doubles
   DevBuf part, sums, stats4, packed, cn, status;
+  // Pencil-pass status word of this handle: set nonzero on the device when a bounded wait of a
+  // pencil pass gave up (check_pipe reads and clears it); and the limit of those waits.
+  DevBuf pipe_st;
+  unsigned long long wait_ns = 1000000000ull;
   DevBuf twid[2];
   int tw_off[2][3] = {};  // offsets of the x, y, z tables in twid
   DevBuf dksq;
@@ -522,6 +526,8 @@ struct System {
     packed.alloc(sizeof(double) * 4096);
     cn.alloc(sizeof(double) * kMaxHist);
     status.alloc(sizeof(int) * 4);
+    pipe_st.alloc(sizeof(int));
+    PF_CU(cudaMemsetAsync(pipe_st.p, 0, sizeof(int), st));
     {
       const double v1 = 1.0;
       one.alloc(sizeof(double));
@@ -735,6 +741,13 @@ struct System {
   // float32 propagators are rescaled per contour step; float64 ones follow the reference as is
   static bool scaled(int p) { return p == 1; }
 
+  // a chain launched by this handle reports its pencil-pass timeouts to the handle's word
+  template <typename T>
+  void own(ChainHost<T>& h) const {
+    h.status = pipe_st.as<int>();
+    h.wait_ns = wait_ns;
+  }
+
   // ---------------------------------------------------------------- propagator setup
   template <typename T>
   void ensure_prop(int p) {
@@ -816,6 +829,7 @@ struct System {
         h.csc = dir ? c1 : c0;
         h.lsc = dir ? l1 : l0;
         h.nsteps = sp.Ns;
+        own(h);
         hosts.push_back(h);
       }
       maxsteps = std::max(maxsteps, sp.Ns);
@@ -890,6 +904,8 @@ struct System {
     h1.ld = ld1;
     h2.nsteps = 2;
     h2.ld = ld2;
+    own(h1);
+    own(h2);
     launch_chains<double>(jd, 1, 1, dims, tw<double>(0), st, &h1);
     launch_chains<double>(jd + 1, 1, 2, dims, tw<double>(0), st, &h2);
     launch_rqm4_combine<double>(y, X + ng, Y + 2 * ng, ng, st);
@@ -1080,13 +1096,18 @@ struct System {
       if (sp->kind == 0) steps += (double)sp->Ns * (sp->nblocks() > 1 ? 2 : 1);
     return (double)ng * std::max(1.0, steps);
   }
-  // A pencil-pass pipeline that gave up waiting on a TMA copy leaves a device flag.
-  void check_pipe(int p) {
-    if (nz == 1) return;
-    const int ps = p == 1 ? take_pipe_status<float>(st) : take_pipe_status<double>(st);
-    if (ps)
-      throw PFError(E_CUDA, "pencil pass: a TMA copy did not complete within its time limit; the last density "
-                            "solve is invalid");
+  // A pencil pass that gave up waiting on a TMA copy sets this handle's status word; read and
+  // clear it (synchronises the handle's stream) and report PF_ETIMEOUT.
+  void check_pipe(int = 0) {
+    int v = 0;
+    if (nz > 1) {  // 1D/2D chains have no pencil pass
+      PF_CU(cudaMemcpyAsync(&v, pipe_st.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+      PF_CU(cudaMemsetAsync(pipe_st.p, 0, sizeof(int), st));
+    }
+    PF_CU(cudaStreamSynchronize(st));
+    if (v)
+      throw PFError(E_TIMEOUT, "pencil pass: a TMA copy did not complete within its time limit; the last density "
+                               "solve is invalid");
   }
   void fetch_Q() {
     for (auto& sp : species) {
@@ -1123,7 +1144,7 @@ struct System {
     check_launch();
     double s[4];
     PF_CU(cudaMemcpyAsync(s, stats4.p, sizeof(s), cudaMemcpyDeviceToHost, st));
-    PF_CU(cudaStreamSynchronize(st));
+    check_pipe();  // also synchronises: a timed-out pencil pass invalidates these sums
     ferr = std::sqrt(s[0]) / std::sqrt(2.220446049250313e-16 + s[1]);
     double ftrans = 0.0;
     for (auto& sp : species) {
@@ -1667,6 +1688,7 @@ struct System {
         h.kbuf = nz > 1 ? k1 : nullptr;
         h.nsteps = 1;
         h.ld = &ldb;
+        own(h);
         launch_chains<T>(jd + job, 1, 1, dims, tw<T>(p), st, &h);
         launch_adj_finish<T>(lam, rr, lam, x, y, G.as<double>() + (size_t)b * ng, cfac, src, ng, st);
         check_launch();
@@ -1693,6 +1715,7 @@ struct System {
         h.lsc = scaled(p) ? seglsc.as<double>() : nullptr;
         h.nsteps = std::min(K, Ns - c * K);
         h.ld = lds_of<T>()[jobidx + ch].data() + c * K;
+        own(h);
         launch_chains<T>(segjobs.as<ChainJob<T>>() + ch * nseg + c, 1, h.nsteps, dims, tw<T>(p), st, &h);
         check_launch();
         return static_cast<const T*>(B);
@@ -1917,6 +1940,7 @@ struct System {
     ChainHost<T> host;
     host.kbuf = kp;
     host.nsteps = nsteps;
+    own(host);
     host.ld = ld_steps.data();
     launch_chains<T>(job.as<ChainJob<T>>(), 1, nsteps, GridDims{nx, ny, nz}, tw<T>(p), st, &host);
     check_launch();
@@ -2365,6 +2389,16 @@ int pf_propagate(pf_system* sys, const double* omega, double vol, double b, doub
     if (!omega || !qin || !qout) throw pf::PFError(PF_EARG, "null array");
     if (s.prec == 0) s.propagate_t<double>(0, omega, vol, b, ds, qin, qout, nsteps);
     else s.propagate_t<float>(1, omega, vol, b, ds, qin, qout, nsteps);
+  });
+}
+
+int pf_set_wait_limit(pf_system* sys, double seconds) {
+  return guard(sys, [&](pf::System& s) {
+    if (!(seconds >= 0.0) || seconds > 10.0) throw pf::PFError(pf::E_ARG, "wait limit must be in [0, 10] seconds");
+    s.wait_ns = (unsigned long long)(seconds * 1e9);
+    for (auto& h : s.hosts_f) h.wait_ns = s.wait_ns;
+    for (auto& h : s.hosts_d) h.wait_ns = s.wait_ns;
+    s.invalidate_graphs();  // captured launches hold the old limit
   });
 }
 

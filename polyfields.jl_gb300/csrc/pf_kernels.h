@@ -111,6 +111,13 @@ struct ChainHost {
   double* lsc = nullptr;
   int nsteps = 0;
   const T* const* ld = nullptr;  // bond operator of each step (host array of nsteps pointers)
+  // Device status word of the chain's owner (a handle, or the allocation-free entry point's
+  // scratch array): the pencil pass sets it nonzero when one of its bounded waits on a TMA copy
+  // gave up (that launch's output is invalid).  Null: not reported.
+  int* status = nullptr;
+  // Time limit (ns of GPU time) of the pencil pass's waits for its tiles; 0 makes them give up
+  // at once (failure tests).  The drain of copies in flight keeps the default limit.
+  unsigned long long wait_ns = 1000000000ull;
 };
 // 3D grids need hosts (njobs entries); 1D/2D grids ignore it.
 template <typename T>
@@ -171,10 +178,6 @@ void launch_nag_update(double* w, const double* temp, double* m, const double* r
 // RQM4: out = (4 q2 - q1) / 3 (pf_adjoint.cu)
 template <typename T>
 void launch_rqm4_combine(T* out, const T* q1, const T* q2, long n, cudaStream_t st);
-// Nonzero when a pipelined kernel of this precision gave up waiting on a copy since the
-// last call (reads and clears a device flag; synchronises the stream).
-template <typename T>
-int take_pipe_status(cudaStream_t st);
 // Stress sums: Nz == 1 uses items (device array of nitems); 3D grids use the pointer arrays
 // src_q/src_qc (real grids) and kq/kqc (half-spectrum scratch), each nitems long.
 template <typename T>

@@ -620,9 +620,8 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, sizeof(T) == 8 ? 1 
 // zrow_perm, that spreads each group's accesses over the banks under the swizzle); after LD and
 // the inverse transform the tile goes back to global memory with one TMA store.  Each CTA runs
 // several tiles through STAGES buffers, so copies of the next tiles overlap the transforms.
-// Nonzero when a bounded wait of the pencil pipeline gave up; that launch's output is invalid.
-// Read and cleared by the host.
-static __device__ int g_pipe_status;
+// When a bounded wait gives up, the launch writes 1 to its owner's status word (a per-handle
+// device int, read and cleared by the host) and its output is invalid.
 
 template <typename T, int NZ>
 struct ZPipe {
@@ -752,11 +751,14 @@ __device__ __forceinline__ void ztile_inverse(Cx<T>* kt, int m, int g, const Cx<
 
 // One contour step's pencil pass of one chain: forward z, LD (and, for tile 0, the rescale
 // factor of the step from the (0,0,0) coefficient), inverse z.  kmap views the chain's
-// half-spectrum scratch as rows of Nkp elements (8-byte units), lmap the step's LD.
+// half-spectrum scratch as rows of Nkp elements (8-byte units), lmap the step's LD.  A wait
+// for a tile that gives up after wait_ns sets *status (when not null); the copies already
+// issued are then drained with the default limit before the CTA exits.
 template <typename T, int NZ>
 __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
     z_pipe_kernel(const __grid_constant__ CUtensorMap kmap, const __grid_constant__ CUtensorMap lmap,
-                  float* __restrict__ csc, double* __restrict__ lsc, int t, int ntiles, double ng, Twiddles<T> twg) {
+                  float* __restrict__ csc, double* __restrict__ lsc, int t, int ntiles, double ng, Twiddles<T> twg,
+                  int* __restrict__ status, unsigned long long wait_ns) {
   using Z = ZPipe<T, NZ>;
   constexpr int S = Z::STAGES, TPC = Z::TPC, G = Z::G;
   extern __shared__ unsigned char smem_raw[];
@@ -802,7 +804,7 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
 #pragma unroll 1
   for (int k = 0; k < nk; ++k) {
     const int s = k % S, r = (int)blockIdx.x + k * (int)gridDim.x;
-    const bool good = mbar_wait(&full[s], (unsigned)((k / S) & 1));
+    const bool good = mbar_wait(&full[s], (unsigned)((k / S) & 1), wait_ns);
     if (__syncthreads_or(!good)) {
       ok = false;
       break;
@@ -847,8 +849,8 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
   if (threadIdx.x == 0) {
     bulk_wait<0>();
     if (!ok) {
-      g_pipe_status = 1;
-      // drain the copies still in flight into this CTA's stages (bounded waits)
+      if (status) *status = 1;
+      // drain the copies still in flight into this CTA's stages (bounded waits, default limit)
       const int issued = min(nk, waited + S - 1);
       for (int k = waited; k < issued; ++k) mbar_wait(&full[k % S], (unsigned)((k / S) & 1));
     }
@@ -1260,7 +1262,7 @@ static void launch_z_pipe(const ChainHost<T>& h, int t, int nkp, double ng, cons
   if (grid > grid_cap) grid = grid_cap;
   if (grid < 1) grid = 1;
   launch_on(z_pipe_kernel<T, NZ>, dim3(grid), dim3(Z::THREADS), Z::SMEM, st, true, km, lm, h.csc, h.lsc, t,
-            ntiles, ng, tw);
+            ntiles, ng, tw, h.status, h.wait_ns);
   count_launches(1);
 }
 
@@ -1277,16 +1279,6 @@ static void z_pipe_dispatch(int nz, const ChainHost<T>& h, int t, int nkp, doubl
     default:
       return;
   }
-}
-
-template <typename T>
-int take_pipe_status(cudaStream_t st) {
-  int v = 0;
-  const int zero = 0;
-  cudaMemcpyFromSymbolAsync(&v, g_pipe_status, sizeof(int), 0, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyToSymbolAsync(g_pipe_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st);
-  cudaStreamSynchronize(st);
-  return v;
 }
 
 template <typename T, int NX, int NY>
@@ -1512,7 +1504,6 @@ void launch_stress(const StressItem<T>* items, int nitems, const T* const* src_q
   template void launch_fill<T>(T*, T, long, cudaStream_t);                                                \
   template void launch_chains<T>(const ChainJob<T>*, int, int, const GridDims&, const Twiddles<T>&,       \
                                  cudaStream_t, const ChainHost<T>*, const Branches*);                     \
-  template int take_pipe_status<T>(cudaStream_t);                                                          \
   template int launch_grad_transform<T>(const T*, const T*, Cx<T>*, Cx<T>*, const T* const*, Cx<T>* const*,   \
                                         const GridDims&, const double*, int, double*, const Twiddles<T>&,     \
                                         cudaStream_t);                                                          \

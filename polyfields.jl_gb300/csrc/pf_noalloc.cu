@@ -12,7 +12,10 @@
 // Every call uses the same array: two calls whose work overlaps on the GPU (different
 // streams, or different host threads) race on it and must be serialised by the caller.
 // Nothing in the array needs clearing between calls: each call writes every byte it later
-// reads (descriptors and twiddles by copy, the half spectrum by the first plane pass).
+// reads (descriptors and twiddles by copy, the half spectrum by the first plane pass).  The
+// one exception is the status word: a 3D pencil pass whose bounded wait for a TMA copy gave
+// up sets it (the call's output is then invalid); it starts at zero when the library loads,
+// stays set across calls, and pf_propagate_noalloc_status reads and clears it.
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -26,6 +29,7 @@ namespace {
 
 constexpr size_t kScratchBytes = size_t(16) << 20;  // 16 MiB
 constexpr size_t kJobOffset = 0;                     // one ChainJob
+constexpr size_t kStatusOffset = 1024;               // the pencil passes' status word (int)
 constexpr size_t kOpsOffset = 4096;                  // StepOp table
 constexpr size_t kTwOffset = 64 * 1024;              // twiddle tables for x, y, z
 constexpr size_t kKbufOffset = 96 * 1024;            // half-spectrum buffer (3D)
@@ -102,6 +106,7 @@ int propagate_noalloc(int nx, int ny, int nz, T* hist, const T* lw, const T* ld,
   host.kbuf = kbuf;
   host.nsteps = nsteps;
   host.ld = ld_steps.data();
+  host.status = reinterpret_cast<int*>(b + kStatusOffset);
   try {
     launch_chains<T>(job_dev, 1, nsteps, GridDims{nx, ny, nz}, tw, st, &host);
   } catch (const DeviceError& e) {
@@ -112,6 +117,20 @@ int propagate_noalloc(int nx, int ny, int nz, T* hist, const T* lw, const T* ld,
     return E_ARG;
   }
   return cudaGetLastError() == cudaSuccess ? OK : E_CUDA;
+}
+
+// Reads the status word on stream st, waits for st, clears the word.
+int take_status(cudaStream_t st, int* out) {
+  void* base = nullptr;
+  const int rc = scratch_address(&base);
+  if (rc != OK) return rc;
+  int* word = reinterpret_cast<int*>(static_cast<unsigned char*>(base) + kStatusOffset);
+  int v = 0;
+  if (cudaMemcpyAsync(&v, word, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemsetAsync(word, 0, sizeof(int), st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
+    return E_CUDA;
+  *out = v;
+  return OK;
 }
 
 }  // namespace
@@ -137,4 +156,11 @@ extern "C" int pf_propagate_noalloc(int nx, int ny, int nz, int precision, void*
                                         static_cast<const float*>(ld), nsteps, st);
   }
   return PF_EARG;
+}
+
+extern "C" int pf_propagate_noalloc_status(void* stream) {
+  int v = 0;
+  const int rc = pf::take_status(static_cast<cudaStream_t>(stream), &v);
+  if (rc != pf::OK) return rc;
+  return v ? PF_ETIMEOUT : PF_OK;
 }

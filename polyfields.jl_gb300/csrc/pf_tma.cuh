@@ -56,13 +56,19 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Wait for the phase with the given parity to complete; false after ~1 s (or 2^26 polls).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+// Default limit of a bounded wait: about a second of GPU time.
+constexpr uint64_t kWaitLimitNs = 1000000000ull;
+
+// Wait for the phase with the given parity to complete; false after limit_ns of GPU time (or
+// 2^26 polls).  A limit of 0 gives up at once without polling (used to exercise the timeout
+// path of a kernel in tests; the copies the barrier tracks still complete).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, uint64_t limit_ns = kWaitLimitNs) {
+  if (limit_ns == 0) return false;
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   for (unsigned n = 1; n < (1u << 26); ++n) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((n & 255) == 0 && global_ns() - t0 > 1000000000ull) return false;
+    if ((n & 255) == 0 && global_ns() - t0 > limit_ns) return false;
   }
   return false;
 }

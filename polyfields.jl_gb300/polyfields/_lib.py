@@ -83,6 +83,8 @@ SIGNATURES = {
                                ctypes.POINTER(ScftResults), ctypes.POINTER(_c_int), _c_int]),
     "pf_propagate": (_c_int, [_vp, _dptr, _c_double, _c_double, _c_double, _dptr, _dptr, _c_int]),
     "pf_propagate_noalloc": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _c_int, _vp]),
+    "pf_propagate_noalloc_status": (_c_int, [_vp]),
+    "pf_set_wait_limit": (_c_int, [_vp, _c_double]),
     "pf_set_timing": (_c_int, [_vp, _c_int]),
     "pf_last_timing": (_c_int, [_vp, _dptr, _dptr, _iptr]),
     "pf_record_event": (_c_int, [_vp, _c_int]),

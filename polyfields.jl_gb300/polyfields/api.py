@@ -423,6 +423,13 @@ class FieldSystem:
                 out["chi"][pair] = 0.0
         return out
 
+    def set_wait_limit(self, seconds: float) -> None:
+        """Time limit of the 3D pencil passes' bounded waits for their TMA copies (default 1 s).
+        A wait that runs out invalidates the solve: the next call that reads results raises
+        PolyFieldsError with status PF_ETIMEOUT, and the handle stays usable.  0 makes every
+        such wait give up at once (exercises the timeout path in tests)."""
+        L.check(L.load().pf_set_wait_limit(self._h, float(seconds)), self._h)
+
     def set_timing(self, enable: bool) -> None:
         L.check(L.load().pf_set_timing(self._h, 1 if enable else 0), self._h)
 

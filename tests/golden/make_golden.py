@@ -9,7 +9,7 @@ run of its usage section (README.md:62-79).  This script converts the seeds to c
 checkout is absent.  The published scalars the tests compare against are constants in
 ``tests/golden/reference_values.py`` with the file and cell they come from.
 
-Usage:  python tests/golden/make_golden.py [path/to/PolyFields.jl]
+Usage:  python tests/golden/make_golden.py path/to/PolyFields.jl
 """
 import json
 import os
@@ -34,7 +34,9 @@ def convert(src: str, dst: str) -> None:
 
 
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_golden.py path/to/PolyFields.jl")
+    ref = sys.argv[1]
     for name in ("lam1d", "cyl2d", "abc_blend_1d"):
         convert(os.path.join(ref, "examples", "seeds", f"{name}.json"), os.path.join(HERE, f"seed_{name}.npz"))
 
