@@ -109,79 +109,71 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline_sample(min_seconds=10.0):
-    """The FP64 CPU restatement (oracle, NumPy + pocketfft on all cores) on a bounded sample of
-    the same workload: contour steps of the 128^3 propagator for at least min_seconds, scaled
-    to one SCFT iteration (600 contour steps).  The Simpson integration and the Anderson
-    update are not in the sample, so the CPU rate is an upper bound."""
+def cpu_blend(n=N_GRID, seed=12345):
+    """The benchmark workload held by the C++/OpenMP FP64 CPU restatement (oracle/pf_cpu.cpp), on
+    all host threads, with the Anderson updater (nhist 20) set up."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import numpy as np
+    import pf_cpu as C
     import pf_oracle as O
-    O.FFT_WORKERS = -1
-    dims = (N_GRID,) * 3
-    cell = O.UnitCell(3, "cubic", 14.0)
-    cell.setup(dims)
-    solver = O.PseudoSpectralSolver(dims)
-    rng = np.random.Generator(np.random.PCG64(12345))
-    w = 0.05 * rng.standard_normal(solver.shape)
-    solver.update(w, cell.ksq, 1.0, 1.0, 0.5)
-    q = np.ones(solver.shape)
-    out = np.empty_like(q)
-    solver.propagate(q, out)
+    from polyfields import workloads as W
+    o = W.blend3d_system(O, n=n, inject=False)  # configuration only: no NumPy density solve
+    c = C.CpuSystem.from_oracle(o)
+    for mid, w in W.blend3d_fields(n, seed).items():
+        c.set_field(mid, w)
+    del o
+    c.anderson_setup(NHIST)
+    return c
+
+
+CPU_KIND = "port"
+CPU_SAMPLE = ("one scft! iteration of the 128^3 blend (density: 600 contour steps with the project's FFT, Simpson, "
+              "residuals, free energy, field error; Anderson step) in the C++17/OpenMP FP64 CPU restatement "
+              "(oracle/pf_cpu.cpp)")
+
+
+def cpu_baseline_sample(warm=1, timed=1):
+    """The C++/OpenMP FP64 CPU restatement on a bounded sample of the same workload: `timed` full
+    SCFT iterations (after `warm` untimed ones: the first is the Anderson updater's Euler step)
+    on all host threads.  The Anderson history then holds `warm` entries, so the Gram sums of a
+    full 20-entry history (under 2% of an iteration here) are not in the sample."""
+    c = cpu_blend()
+    for _ in range(warm):
+        c.anderson_step()
     t0 = time.perf_counter()
-    nsteps = 0
-    while nsteps < 10 or time.perf_counter() - t0 < min_seconds:
-        solver.propagate(q, out)
-        q, out = out, q
-        nsteps += 1
-    dt = time.perf_counter() - t0
-    return {"value": (nsteps / dt) / MDE_STEPS_PER_ITER, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{nsteps} contour steps of the 128^3 FP64 propagator (NumPy/pocketfft, FFTs on all cores, "
-                      f"elementwise single-threaded) in {dt:.1f} s, scaled to 600 steps per iteration",
-            "mde_steps_per_s": nsteps / dt}
+    for _ in range(timed):
+        c.anderson_step()
+        c.free_energy()
+        c.field_error()
+    dt = (time.perf_counter() - t0) / timed
+    return {"value": 1.0 / dt, "unit": UNIT, "cores": c.threads, "kind": CPU_KIND,
+            "sample": f"{timed} x " + CPU_SAMPLE + f" after {warm} warm-up iteration(s): {dt:.1f} s per iteration",
+            "mde_steps_per_s": MDE_STEPS_PER_ITER / dt}
 
 
 def run_reference(args):
-    """Reference arm: the FP64 CPU restatement of the reference's path (the oracle); each step
-    is a bounded sample (100 contour steps of the 128^3 propagator) scaled to iterations/s."""
+    """Reference arm: the reference (Julia + FFTW) cannot run here, so this times its FP64 CPU
+    restatement in C++/OpenMP (oracle/pf_cpu.cpp) on all host threads, one full scft!
+    iteration of the benchmark workload per step."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import numpy as np
-    import pf_oracle as O
-    O.FFT_WORKERS = -1
-    dims = (N_GRID,) * 3
-    cell = O.UnitCell(3, "cubic", 14.0)
-    cell.setup(dims)
-    solver = O.PseudoSpectralSolver(dims)
-    rng = np.random.Generator(np.random.PCG64(12345))
-    solver.update(0.05 * rng.standard_normal(solver.shape), cell.ksq, 1.0, 1.0, 0.5)
-    q = np.ones(solver.shape)
-    out = np.empty_like(q)
-    per_step = 100
-
-    def one():
-        nonlocal q, out
-        for _ in range(per_step):
-            solver.propagate(q, out)
-            q, out = out, q
-
-    for _ in range(args.warmup):
-        one()
+    c = cpu_blend()
+    for _ in range(max(1, args.warmup)):
+        c.anderson_step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        one()
+        c.anderson_step()
+        c.free_energy()
+        c.field_error()
     dt = time.perf_counter() - t0
-    steps_per_s = per_step * args.steps / dt
-    value = steps_per_s / MDE_STEPS_PER_ITER
-    sample = (f"{per_step} contour steps of the 128^3 FP64 propagator per step (NumPy/pocketfft, FFTs on all cores), "
-              f"scaled to 600 contour steps per SCFT iteration; Simpson and Anderson work not included")
+    value = args.steps / dt
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": WORKLOAD, "mde_steps_per_s": steps_per_s,
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": sample},
+            "data": "synthetic", "config": dict(WORKLOAD, size=N_GRID),
+            "mde_steps_per_s": value * MDE_STEPS_PER_ITER,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": c.threads, "kind": CPU_KIND,
+                             "sample": CPU_SAMPLE + " per step"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -299,7 +291,7 @@ def run_gpu(args):
         fp64 = {"iters_per_s": 1000.0 * args.fp64_steps / m64.value, "ms_per_iter": m64.value / args.fp64_steps,
                 "mde_step_us": 1000.0 * a64 / nmde}
 
-    cpu = cpu_baseline_sample(args.cpu_seconds) if args.cpu_seconds > 0 else None
+    cpu = cpu_baseline_sample() if args.cpu_seconds > 0 else None
     del upd, sysm
     # time to solution, mixed vs plain FP64, on a grid that fits the run's time (median of seeds)
     tts = tts_summary(args.tts_size, [12345 + 1000 * i for i in range(args.seeds)]) if args.tts_size > 0 else None
@@ -331,7 +323,8 @@ def tts_pair(n, seed, ftol=1e-8, nsteps=4000, switch=3e-6, nhist=NHIST):
         r = pf.scft(sysm, pf.AndersonUpdater(nhist=nhist), opts=opts)
         sysm.synchronize()
         out[mode] = {"wall_s": time.perf_counter() - t0, "iterations": r.nsteps, "converged": bool(r.converged),
-                     "switch_step": r.switch_step, "ferr": r.ferr, "fhelm": r.fhelm}
+                     "switch_step": r.switch_step, "ferr": r.ferr, "fhelm": r.fhelm,
+                     "polish_fp64_solves": r.polish_fp64_solves, "polish_fp32_solves": r.polish_fp32_solves}
         del sysm
     out["wall_ratio"] = out["fp64"]["wall_s"] / out["mixed"]["wall_s"]
     out["abs_dfhelm"] = abs(out["mixed"]["fhelm"] - out["fp64"]["fhelm"])
@@ -342,7 +335,8 @@ def tts_summary(n, seeds):
     runs = [dict(seed=sd, **tts_pair(n, sd)) for sd in seeds]
     ratios = sorted(r["wall_ratio"] for r in runs)
     return {"workload": f"large blend {n}^3 (cell held at L0 = 14), Anderson nhist {NHIST}, ftol 1e-8; mixed = "
-                        f"float32 propagators to ferr 3e-6, then float64 polish",
+                        f"float32 propagators to ferr 3e-6, then Newton-Krylov polish (float64 residuals, "
+                        f"float32 Jacobian products)",
             "seeds": list(seeds), "wall_ratio_median": statistics.median(ratios),
             "wall_ratio_min": ratios[0], "wall_ratio_max": ratios[-1],
             "abs_dfhelm_max": max(r["abs_dfhelm"] for r in runs),
@@ -421,7 +415,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=N_GRID, help="grid points per axis (default 128)")
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="length of the CPU baseline sample (0: skip)")
+    ap.add_argument("--cpu-seconds", type=float, default=1.0, help="CPU baseline sample (0: skip; else one iteration)")
     ap.add_argument("--mode", default="iter", choices=["iter", "tts", "sweep", "profile"])
     ap.add_argument("--seeds", type=int, default=3, help="tts: seeds of the time-to-solution runs")
     ap.add_argument("--tts-size", type=int, default=64,

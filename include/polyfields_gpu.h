@@ -52,18 +52,22 @@ typedef struct pf_system pf_system;
  * mixed_switch_ferr > 0 and the handle runs PF_FP32, scft switches to PF_FP64 once
  * ferr < mixed_switch_ferr, or once the FP32 iterations have not lowered ferr by 1% for 200
  * steps (their rounding floor lies above mixed_switch_ferr), and continues to ftol/stol (FP64
- * polish). */
+ * polish).  polish selects how: 0 = Newton-Krylov steps (each one float64 residual and a
+ * restarted GMRES over float32 finite-difference Jacobian products; runs without a
+ * DomainUpdater; falls back to the field updater's float64 steps if a Newton step stalls),
+ * 1 = float64 steps of the field updater (the Anderson history restarted at the switch). */
 typedef struct pf_scft_options {
   int nsteps;
   int nsout;
   int nsave;
-  int pad0;
+  int polish;
   double ftol;
   double stol;
   double mixed_switch_ferr;
 } pf_scft_options;
 
-/* SCFTResults (src/simulate.jl:26-33) plus the step at which the precision switched (-1 if never). */
+/* SCFTResults (src/simulate.jl:26-33) plus the step at which the precision switched (-1 if
+ * never) and the density solves of a Newton-Krylov polish (float64 and float32). */
 typedef struct pf_scft_results {
   double time;
   int nsteps;
@@ -72,6 +76,8 @@ typedef struct pf_scft_results {
   double serr;
   double fhelm;
   int switch_step;
+  int polish_fp64_solves;
+  int polish_fp32_solves;
   int pad0;
 } pf_scft_results;
 

@@ -17,7 +17,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 OUT = os.path.join(HERE, "polyfields", "libpolyfields_gpu.so")
-SOURCES = ["pf_mde_fp32.cu", "pf_mde_fp64.cu", "pf_field.cu", "pf_engine.cu", "pf_noalloc.cu", "pf_adjoint.cu"]
+SOURCES = ["pf_mde_fp32.cu", "pf_mde_fp64.cu", "pf_field.cu", "pf_engine.cu", "pf_noalloc.cu", "pf_adjoint.cu",
+           "pf_polish.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]

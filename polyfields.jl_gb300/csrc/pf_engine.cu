@@ -1406,6 +1406,171 @@ struct System {
     and_.lam = 0.0;
   }
 
+  // ---------------------------------------------------------------- Newton-Krylov polish
+  // The float64 phase of a mixed run, as inexact Newton steps on F64(w) = 0 (F = residuals!
+  // with float64 propagators): w <- w + delta with J delta = -F64(w) solved by restarted GMRES
+  // whose Jacobian-vector products are finite differences of float32 residuals about w,
+  //   J v ~ (F32(w + e v) - F32(w)) / e,   e |v| = kNKStep |w|.
+  // A perturbation of 1% of the field keeps float32 rounding (ferr ~ 1e-6 of |w|) below 1e-3
+  // of each product, which is accurate enough for Newton steps that each shrink ferr by a
+  // factor ~20-50; only the acceptance test and the right-hand side are float64 solves.  The
+  // fixed point is the reference's: a run ends only when the float64 ferr < ftol.
+  static constexpr int kNKRestart = 30;      // GMRES restart length
+  static constexpr int kNKMaxMatvec = 240;   // float32 products per Newton step at most
+  static constexpr double kNKStep = 1e-2;
+  struct NKBufs {
+    DevBuf V, wk, r64, r32, z, delta, h, part;
+  } nkb;
+  int nk_fp32 = 0, nk_fp64 = 0;
+
+  double nk_dot(const double* a, const double* b, long n) {
+    double* hd = nkb.h.as<double>() + 3 * (kNKRestart + 2);
+    launch_multidot(a, 1, n, b, nkb.part.as<double>(), hd, st);
+    double v = 0.0;
+    PF_CU(cudaMemcpyAsync(&v, hd, sizeof(double), cudaMemcpyDeviceToHost, st));
+    PF_CU(cudaStreamSynchronize(st));
+    return v;
+  }
+  // z = (F32(wk + e v) - F32(wk)) / e with e = kNKStep |wk| / vnorm
+  void nk_jvp(const double* v, double vnorm, double wnorm, long n) {
+    const double e = kNKStep * wnorm / vnorm;
+    double* wp = w.as<double>();
+    PF_CU(cudaMemcpyAsync(wp, nkb.wk.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    launch_lincomb(wp, v, 1.0, e, n, st);
+    prec = 1;
+    residuals();
+    double* z = nkb.z.as<double>();
+    PF_CU(cudaMemcpyAsync(z, res.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    launch_lincomb(z, nkb.r32.as<double>(), 1.0 / e, -1.0 / e, n, st);
+    check_launch();
+    ++nk_fp32;
+  }
+  // Returns true once the float64 ferr < ftol; false when a Newton step did not shrink ferr
+  // (the fields are then the last accepted ones and the caller goes on with float64 steps of
+  // its field updater).  Each Newton step counts as one scft! step.
+  bool nk_polish(const pf_scft_options& o, int& step, double& ferr, double& fhelm) {
+    const long n = (long)nmon() * ng;
+    const int m = kNKRestart;
+    nkb.V.alloc(sizeof(double) * n * (m + 1));
+    for (DevBuf* b : {&nkb.wk, &nkb.r64, &nkb.r32, &nkb.z, &nkb.delta}) b->alloc(sizeof(double) * n);
+    nkb.h.alloc(sizeof(double) * 4 * (m + 2));
+    nkb.part.alloc(sizeof(double) * polish_part_doubles());
+    double* V = nkb.V.as<double>();
+    double* hd = nkb.h.as<double>();
+    double* wk = nkb.wk.as<double>();
+    double* r64 = nkb.r64.as<double>();
+    double* z = nkb.z.as<double>();
+    double* delta = nkb.delta.as<double>();
+    prec = 0;
+    residuals();
+    stats(ferr, fhelm);
+    ++nk_fp64;
+    int poor = 0;
+    std::vector<double> H((size_t)(m + 1) * m), g(m + 1), cs(m), sn(m), y(m), hh(2 * (m + 1) + 1);
+    while (ferr >= o.ftol && step < o.nsteps) {
+      PF_CU(cudaMemcpyAsync(wk, w.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      PF_CU(cudaMemcpyAsync(r64, res.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      const double beta = std::sqrt(nk_dot(r64, r64, n));
+      const double wnorm = std::sqrt(nk_dot(wk, wk, n));
+      // float32 residual at the linearisation point
+      prec = 1;
+      residuals();
+      PF_CU(cudaMemcpyAsync(nkb.r32.p, res.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      ++nk_fp32;
+      const double eta = std::min(0.3, std::max(1e-2, 0.3 * o.ftol / ferr));  // forcing term
+      PF_CU(cudaMemsetAsync(delta, 0, sizeof(double) * n, st));
+      // first cycle: V_0 = -r64 / beta
+      PF_CU(cudaMemcpyAsync(V, r64, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      launch_lincomb(V, V, -1.0 / beta, 0.0, n, st);
+      double rcur = beta;
+      int matvecs = 0;
+      for (;;) {
+        std::fill(g.begin(), g.end(), 0.0);
+        g[0] = rcur;
+        int jl = -1;
+        double resid = rcur;
+        for (int j = 0; j < m; ++j) {
+          nk_jvp(V + (long)j * n, 1.0, wnorm, n);
+          ++matvecs;
+          // classical Gram-Schmidt, twice
+          launch_multidot(V, j + 1, n, z, nkb.part.as<double>(), hd, st);
+          launch_multiaxpy(z, V, j + 1, n, hd, 1.0, -1.0, st);
+          launch_multidot(V, j + 1, n, z, nkb.part.as<double>(), hd + (m + 1), st);
+          launch_multiaxpy(z, V, j + 1, n, hd + (m + 1), 1.0, -1.0, st);
+          launch_multidot(z, 1, n, z, nkb.part.as<double>(), hd + 2 * (m + 1), st);
+          check_launch();
+          PF_CU(cudaMemcpyAsync(hh.data(), hd, sizeof(double) * (2 * (m + 1) + 1), cudaMemcpyDeviceToHost, st));
+          PF_CU(cudaStreamSynchronize(st));
+          for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hh[i] + hh[m + 1 + i];
+          const double hn = std::sqrt(std::max(0.0, hh[2 * (m + 1)]));
+          H[(size_t)(j + 1) * m + j] = hn;
+          if (hn > 0.0) {
+            PF_CU(cudaMemcpyAsync(V + (long)(j + 1) * n, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+            launch_lincomb(V + (long)(j + 1) * n, z, 1.0 / hn, 0.0, n, st);
+          }
+          for (int i = 0; i < j; ++i) {  // earlier Givens rotations on column j
+            const double a = H[(size_t)i * m + j], b = H[(size_t)(i + 1) * m + j];
+            H[(size_t)i * m + j] = cs[i] * a + sn[i] * b;
+            H[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * b;
+          }
+          const double a = H[(size_t)j * m + j], b = H[(size_t)(j + 1) * m + j];
+          const double rr = std::hypot(a, b);
+          cs[j] = rr > 0.0 ? a / rr : 1.0;
+          sn[j] = rr > 0.0 ? b / rr : 0.0;
+          H[(size_t)j * m + j] = rr;
+          H[(size_t)(j + 1) * m + j] = 0.0;
+          g[j + 1] = -sn[j] * g[j];
+          g[j] = cs[j] * g[j];
+          jl = j;
+          resid = std::fabs(g[j + 1]);
+          if (resid <= eta * beta || matvecs >= kNKMaxMatvec || hn == 0.0) break;
+        }
+        // delta += V y with H y = g (upper triangular, jl + 1 columns)
+        for (int i = jl; i >= 0; --i) {
+          double s = g[i];
+          for (int k = i + 1; k <= jl; ++k) s -= H[(size_t)i * m + k] * y[k];
+          y[i] = H[(size_t)i * m + i] != 0.0 ? s / H[(size_t)i * m + i] : 0.0;
+        }
+        PF_H2D(hd + 3 * (m + 1), y.data(), sizeof(double) * (jl + 1), st);
+        launch_multiaxpy(delta, V, jl + 1, n, hd + 3 * (m + 1), 1.0, 1.0, st);
+        if (resid <= eta * beta || matvecs >= kNKMaxMatvec) break;
+        // restart from the true linear residual -r64 - J delta
+        const double dn = std::sqrt(nk_dot(delta, delta, n));
+        nk_jvp(delta, dn, wnorm, n);
+        ++matvecs;
+        PF_CU(cudaMemcpyAsync(V, z, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        launch_lincomb(V, r64, -1.0, -1.0, n, st);
+        rcur = std::sqrt(nk_dot(V, V, n));
+        if (!(rcur > 0.0)) break;
+        launch_lincomb(V, V, 1.0 / rcur, 0.0, n, st);
+      }
+      // Newton step, accepted on a float64 residual
+      double* wp = w.as<double>();
+      PF_CU(cudaMemcpyAsync(wp, wk, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+      launch_lincomb(wp, delta, 1.0, 1.0, n, st);
+      prec = 0;
+      residuals();
+      double fe = 0.0, fh = 0.0;
+      stats(fe, fh);
+      ++nk_fp64;
+      step += 1;
+      if (o.nsout > 0)
+        printf("Newton-Krylov step %d: ferr = %8e, fhelm = %.5e (%d float32 products)\n", step, fe, fh, matvecs);
+      if (!(fe < ferr)) {  // no progress: back to the last accepted fields
+        PF_CU(cudaMemcpyAsync(wp, wk, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        residuals();
+        stats(ferr, fhelm);
+        ++nk_fp64;
+        return false;
+      }
+      const bool slow = !(fe < 0.5 * ferr);
+      ferr = fe;
+      fhelm = fh;
+      if (slow && ++poor >= 2) return ferr < o.ftol;
+    }
+    return ferr < o.ftol;
+  }
+
   void anderson_step() {  // anderson.jl:98-228
     if (!and_.is_setup) throw PFError(E_STATE, "AndersonUpdater not set up");
     auto& A = and_;
@@ -1837,6 +2002,7 @@ struct System {
     auto t0 = std::chrono::steady_clock::now();
     pf_scft_results r{};
     r.switch_step = -1;
+    nk_fp32 = nk_fp64 = 0;
     if (active == 0 && !and_.exists) throw PFError(E_STATE, "no field updater created");
     if (vcell && !dom.exists) throw PFError(E_STATE, "no DomainUpdater created");
     validate();
@@ -1892,6 +2058,19 @@ struct System {
           prec = 0;
           r.switch_step = step;
           if (active == 0) anderson_restart();
+          if (o.polish == 0 && !vcell) {
+            // float64 polish by Newton-Krylov steps with float32 Jacobian products
+            step += 1;
+            converged = nk_polish(o, step, ferr, fhelm);
+            if (std::isnan(ferr)) throw PFError(E_NAN, "Diverging field updater -- breaking.");
+            if (converged) {
+              if (o.nsout > 0) printf("Converged @ step = %d: ferr = %8e, fhelm = %.5e\n", step, ferr, fhelm);
+              break;
+            }
+            // a Newton step stalled: float64 iterations of the field updater from here
+            if (active == 0) anderson_restart();
+            continue;
+          }
         }
       }
       step += 1;
@@ -1900,6 +2079,8 @@ struct System {
     stats(ferr, fhelm);
     if (vcell) serr = stress_error();
     r.time = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    r.polish_fp64_solves = nk_fp64;
+    r.polish_fp32_solves = nk_fp32;
     r.nsteps = step;
     r.converged = converged ? 1 : 0;
     r.ferr = ferr;

@@ -241,4 +241,14 @@ void launch_mix(double* w, const HistPtrs& h, int ih, const double* Cn, double l
 // out = a + b (the history sum of an entry in iterations without a mix)
 void launch_add(double* out, const double* a, const double* b, long n, cudaStream_t st);
 
+// ---- Newton-Krylov polish vector primitives (pf_polish.cu); V_i = V + i n, float64
+// out[i] = V_i . z for i < k (device; part needs polish_part_doubles() doubles)
+void launch_multidot(const double* V, int k, long n, const double* z, double* part, double* out, cudaStream_t st);
+// z = alpha z + beta sum_{i<k} c[i] V_i (c on the device)
+void launch_multiaxpy(double* z, const double* V, int k, long n, const double* c, double alpha, double beta,
+                      cudaStream_t st);
+// y = a y + b x
+void launch_lincomb(double* y, const double* x, double a, double b, long n, cudaStream_t st);
+int polish_part_doubles();
+
 }  // namespace pf

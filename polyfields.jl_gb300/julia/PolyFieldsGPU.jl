@@ -27,7 +27,7 @@ struct PFOptions            # pf_scft_options
     nsteps::Cint
     nsout::Cint
     nsave::Cint
-    pad0::Cint
+    polish::Cint              # 0 Newton-Krylov polish, 1 float64 field-updater steps
     ftol::Cdouble
     stol::Cdouble
     mixed_switch_ferr::Cdouble
@@ -41,8 +41,10 @@ mutable struct PFResults    # pf_scft_results
     serr::Cdouble
     fhelm::Cdouble
     switch_step::Cint
+    polish_fp64_solves::Cint
+    polish_fp32_solves::Cint
     pad0::Cint
-    PFResults() = new(0, 0, 0, 0, 0, 0, -1, 0)
+    PFResults() = new(0, 0, 0, 0, 0, 0, -1, 0, 0, 0)
 end
 
 const PF_OK, PF_EARG, PF_ECUDA, PF_ENAN, PF_ESINGULAR, PF_ETIMEOUT = 0, 1, 2, 3, 4, 5
@@ -127,8 +129,8 @@ function pull_state!(sys::FieldSystem, h)
     return sys
 end
 
-pf_options(opts::SCFTOptions, mixed_switch_ferr) =
-    PFOptions(opts.nsteps, opts.nsout, opts.nsave, 0, opts.ftol, opts.stol, mixed_switch_ferr)
+pf_options(opts::SCFTOptions, mixed_switch_ferr; polish::Integer = 0) =
+    PFOptions(opts.nsteps, opts.nsout, opts.nsave, polish, opts.ftol, opts.stol, mixed_switch_ferr)
 
 # scft!(sys, AndersonUpdater; domain, opts) on the GPU (src/simulate.jl:60-148).
 function scft!(sys::FieldSystem, u::AndersonUpdater; domain = nothing, opts::SCFTOptions = SCFTOptions(),

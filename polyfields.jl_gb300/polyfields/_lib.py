@@ -23,13 +23,14 @@ _iptr = ctypes.POINTER(ctypes.c_int)
 
 
 class ScftOptions(ctypes.Structure):
-    _fields_ = [("nsteps", _c_int), ("nsout", _c_int), ("nsave", _c_int), ("pad0", _c_int),
+    _fields_ = [("nsteps", _c_int), ("nsout", _c_int), ("nsave", _c_int), ("polish", _c_int),
                 ("ftol", _c_double), ("stol", _c_double), ("mixed_switch_ferr", _c_double)]
 
 
 class ScftResults(ctypes.Structure):
     _fields_ = [("time", _c_double), ("nsteps", _c_int), ("converged", _c_int), ("ferr", _c_double),
-                ("serr", _c_double), ("fhelm", _c_double), ("switch_step", _c_int), ("pad0", _c_int)]
+                ("serr", _c_double), ("fhelm", _c_double), ("switch_step", _c_int), ("polish_fp64_solves", _c_int),
+                ("polish_fp32_solves", _c_int), ("pad0", _c_int)]
 
 
 SIGNATURES = {

@@ -634,7 +634,11 @@ def step(updater, **kwargs) -> None:
 class SCFTOptions:
     """src/simulate.jl:12-19, plus ``mixed_switch_ferr``: with an fp32 system, iterate in fp32
     until ferr < mixed_switch_ferr (or until 200 fp32 iterations bring no 1% improvement),
-    then continue in fp64 (0 disables the switch)."""
+    then continue in fp64 (0 disables the switch).  ``polish`` selects the fp64 phase:
+    "newton" (Newton-Krylov steps: one fp64 residual each, the linear solve by GMRES over
+    fp32 finite-difference Jacobian products; runs without a DomainUpdater, falls back to the
+    updater's fp64 steps if a Newton step stalls) or "updater" (fp64 steps of the field
+    updater)."""
     nsteps: int = 100
     nsout: int = 0
     nsave: int = 0
@@ -642,6 +646,7 @@ class SCFTOptions:
     stol: float = 1e-4
     savepath: str = ""
     mixed_switch_ferr: float = 0.0
+    polish: str = "newton"
 
 
 @dataclass
@@ -654,6 +659,23 @@ class SCFTResults:
     serr: float
     fhelm: float
     switch_step: int = -1
+    polish_fp64_solves: int = 0
+    polish_fp32_solves: int = 0
+
+
+_POLISH = {"newton": 0, "updater": 1}
+
+
+def _options(opts: "SCFTOptions"):
+    if opts.polish not in _POLISH:
+        raise ValueError(f"polish must be one of {sorted(_POLISH)}")
+    return L.ScftOptions(opts.nsteps, opts.nsout, opts.nsave, _POLISH[opts.polish], opts.ftol, opts.stol,
+                         opts.mixed_switch_ferr)
+
+
+def _results(r) -> "SCFTResults":
+    return SCFTResults(r.time, r.nsteps, bool(r.converged), r.ferr, r.serr, r.fhelm, r.switch_step,
+                       r.polish_fp64_solves, r.polish_fp32_solves)
 
 
 def scft(sys: FieldSystem, updater: AndersonUpdater, domain: Optional[DomainUpdater] = None,
@@ -665,12 +687,12 @@ def scft(sys: FieldSystem, updater: AndersonUpdater, domain: Optional[DomainUpda
     updater._bind(sys)
     if domain is not None:
         domain._bind(sys)
-    o = L.ScftOptions(opts.nsteps, opts.nsout, opts.nsave, 0, opts.ftol, opts.stol, opts.mixed_switch_ferr)
+    o = _options(opts)
     r = L.ScftResults()
     lib = L.load()
     L.check(lib.pf_set_savepath(sys._h, (opts.savepath or "").encode()), sys._h)
     L.check(lib.pf_scft(sys._h, ctypes.byref(o), 1 if domain is not None else 0, ctypes.byref(r)), sys._h)
-    return SCFTResults(r.time, r.nsteps, bool(r.converged), r.ferr, r.serr, r.fhelm, r.switch_step)
+    return _results(r)
 
 
 def scft_batch(systems: Sequence[FieldSystem], updaters: Sequence[AndersonUpdater],
@@ -699,11 +721,11 @@ def scft_batch(systems: Sequence[FieldSystem], updaters: Sequence[AndersonUpdate
         if d is not None:
             d._bind(sys)
     handles = (L._vp * n)(*[s._h for s in systems])
-    o = L.ScftOptions(opts.nsteps, opts.nsout, opts.nsave, 0, opts.ftol, opts.stol, opts.mixed_switch_ferr)
+    o = _options(opts)
     res = (L.ScftResults * n)()
     st = (ctypes.c_int * n)()
     rc = L.load().pf_scft_batch(handles, n, ctypes.byref(o), 1 if use_domain else 0, res, st, int(nthreads))
-    out = [SCFTResults(r.time, r.nsteps, bool(r.converged), r.ferr, r.serr, r.fhelm, r.switch_step) for r in res]
+    out = [_results(r) for r in res]
     if raise_on_error:
         for i in range(n):
             L.check(st[i], systems[i]._h)

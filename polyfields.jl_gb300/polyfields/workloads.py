@@ -79,10 +79,19 @@ def cyl2d_seed_system(M, precision=None):
     return sys
 
 
-def blend3d_system(M, n=32, L=14.0, precision=None, Ns=200, seed=12345):
+def blend3d_fields(n=32, seed=12345):
+    """Start fields of the large-blend workload: the double gyroid sin x cos y + sin y cos z +
+    sin z cos x (x = 2 pi X / L) for w_A, its negative for w_B, plus 0.05 seeded noise."""
+    shape = (n, n, n)
+    z, y, x = np.meshgrid(*(2 * np.pi * np.arange(n) / n for _ in range(3)), indexing="ij")
+    gyr = np.sin(x) * np.cos(y) + np.sin(y) * np.cos(z) + np.sin(z) * np.cos(x)
+    return seeded_fields(shape, [1, 2], seed, 0.05, gyr)
+
+
+def blend3d_system(M, n=32, L=14.0, precision=None, Ns=200, seed=12345, inject=True):
     """The large-blend workload (128^3 at full size): AB diblock N100 fA0.4 (phi 0.8) + A
     homopolymer N50 (phi 0.2), chi 0.2, Ns 200, cubic cell L0 = 14, double-gyroid start
-    w_A = sin x cos y + sin y cos z + sin z cos x (x = 2 pi X / L), w_B = -w_A, + 0.05 noise."""
+    (blend3d_fields).  inject=False returns the system before fieldinit (no density solve)."""
     A, B = M.Monomer(1), M.Monomer(2)
     cell = M.UnitCell(3, "cubic", L)
     sys = _fs(M, (n, n, n), cell, [A, B], precision)
@@ -91,10 +100,8 @@ def blend3d_system(M, n=32, L=14.0, precision=None, Ns=200, seed=12345):
     itx = M.FloryInteraction()
     itx.set_interaction(A, B, 0.2)
     sys.add_interaction(itx)
-    shape = (n, n, n)
-    z, y, x = np.meshgrid(*(2 * np.pi * np.arange(n) / n for _ in range(3)), indexing="ij")
-    gyr = np.sin(x) * np.cos(y) + np.sin(y) * np.cos(z) + np.sin(z) * np.cos(x)
-    M.fieldinit(sys, seeded_fields(shape, [1, 2], seed, 0.05, gyr))
+    if inject:
+        M.fieldinit(sys, blend3d_fields(n, seed))
     return sys
 
 
