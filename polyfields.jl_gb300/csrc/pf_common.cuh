@@ -24,6 +24,16 @@ template <typename T>
 __device__ __forceinline__ Cx<T> operator+(Cx<T> a, Cx<T> b) { return cx<T>(a.x + b.x, a.y + b.y); }
 template <typename T>
 __device__ __forceinline__ Cx<T> operator-(Cx<T> a, Cx<T> b) { return cx<T>(a.x - b.x, a.y - b.y); }
+// float32 complex sums as one packed two-lane instruction (sm_100-family f32x2 arithmetic):
+// both lanes round as two scalar additions would.
+__device__ __forceinline__ Cx<float> operator+(Cx<float> a, Cx<float> b) {
+  const float2 r = __fadd2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y));
+  return cx<float>(r.x, r.y);
+}
+__device__ __forceinline__ Cx<float> operator-(Cx<float> a, Cx<float> b) {
+  const float2 r = __fadd2_rn(make_float2(a.x, a.y), make_float2(-b.x, -b.y));
+  return cx<float>(r.x, r.y);
+}
 template <typename T>
 __device__ __forceinline__ Cx<T> cmul(Cx<T> a, Cx<T> b) {
   return cx<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);

@@ -29,25 +29,36 @@ __device__ __forceinline__ void dft2(Cx<T>& a0, Cx<T>& a1) {
   a1 = t;
 }
 
+// d +- (-i) t for the forward transform, d +- (+i) t for the inverse, written per component so
+// that no lane swap is needed (the complex sums elsewhere are packed two-lane instructions)
+template <typename T, bool INV>
+__device__ __forceinline__ void rot_pair(const Cx<T>& d, const Cx<T>& t, Cx<T>& plus, Cx<T>& minus) {
+  if (INV) {
+    plus = cx<T>(d.x - t.y, d.y + t.x);
+    minus = cx<T>(d.x + t.y, d.y - t.x);
+  } else {
+    plus = cx<T>(d.x + t.y, d.y - t.x);
+    minus = cx<T>(d.x - t.y, d.y + t.x);
+  }
+}
+
 template <typename T, bool INV>
 __device__ __forceinline__ void dft3(Cx<T>& a0, Cx<T>& a1, Cx<T>& a2) {
   const T s3 = (T)0.866025403784438646763723170752936183;  // sqrt(3)/2
   const Cx<T> t1 = a1 + a2;
   const Cx<T> t2 = cx<T>(a0.x - (T)0.5 * t1.x, a0.y - (T)0.5 * t1.y);
-  const Cx<T> t3 = mul_mi<T, INV>(cscale(a1 - a2, s3));
+  const Cx<T> t3 = cscale(a1 - a2, s3);
   a0 = a0 + t1;
-  a1 = t2 + t3;
-  a2 = t2 - t3;
+  rot_pair<T, INV>(t2, t3, a1, a2);  // t2 +- (-i or +i) t3
 }
 
 template <typename T, bool INV>
 __device__ __forceinline__ void dft4(Cx<T>& a0, Cx<T>& a1, Cx<T>& a2, Cx<T>& a3) {
   const Cx<T> s02 = a0 + a2, d02 = a0 - a2;
-  const Cx<T> s13 = a1 + a3, d13 = mul_mi<T, INV>(a1 - a3);
+  const Cx<T> s13 = a1 + a3, t13 = a1 - a3;
   a0 = s02 + s13;
   a2 = s02 - s13;
-  a1 = d02 + d13;
-  a3 = d02 - d13;
+  rot_pair<T, INV>(d02, t13, a1, a3);
 }
 
 // a * (c - i s) for forward transforms, a * (c + i s) for inverse ones
@@ -83,14 +94,12 @@ __device__ __forceinline__ void dft8(Cx<T>* a) {
   dft4<T, INV>(e0, e1, e2, e3);
   dft4<T, INV>(o0, o1, o2, o3);
   const Cx<T> w1o = wmul<T, INV>(o1, r, r);
-  const Cx<T> w2o = mul_mi<T, INV>(o2);
   const Cx<T> w3o = wmul<T, INV>(o3, -r, r);
   a[0] = e0 + o0;
   a[4] = e0 - o0;
   a[1] = e1 + w1o;
   a[5] = e1 - w1o;
-  a[2] = e2 + w2o;
-  a[6] = e2 - w2o;
+  rot_pair<T, INV>(e2, o2, a[2], a[6]);  // o2 times -i (forward) / +i (inverse)
   a[3] = e3 + w3o;
   a[7] = e3 - w3o;
 }

@@ -614,12 +614,15 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, sizeof(T) == 8 ? 1 
 
 // ------------------------------------------------------------------ 3D: pencil pass through TMA
 // The pencil pass as a pipeline: a tile is M pencils (M * sizeof(Cx<T>) = 128 bytes, one row
-// per z) brought into shared memory by one 2D TMA copy with the 128-byte swizzle, together with
-// the matching LD tile (64-byte rows, 64-byte swizzle).  The forward transform reads the rows
-// in natural order and works in place on the tile (intermediate passes in a permuted row order,
-// zrow_perm, that spreads each group's accesses over the banks under the swizzle); after LD and
-// the inverse transform the tile goes back to global memory with one TMA store.  Each CTA runs
-// several tiles through STAGES buffers, so copies of the next tiles overlap the transforms.
+// per z) brought into shared memory by one 2D TMA copy, together with the matching LD tile (M
+// values of T per row).  Lanes are assigned pencil-major: thread lt of a tile works on pencil
+// m = lt % M as member g = lt / M of that pencil's G-thread group, so a warp touches whole
+// 128-byte rows (M lanes per row) and every shared-memory access is conflict-free without a
+// swizzle; an element's address is the thread's base plus a compile-time offset.  The G
+// threads of a pencil sit in different warps, so the transform passes, which work in place on
+// the tile, separate their loads from their stores with block barriers.  Each CTA runs several
+// tiles through STAGES buffers; the copies of round k + STAGES - 1 are issued when round k
+// starts, so they overlap its transforms.
 // When a bounded wait gives up, the launch writes 1 to its owner's status word (a per-handle
 // device int, read and cleared by the host) and its output is invalid.
 
@@ -632,120 +635,96 @@ struct ZPipe {
   static constexpr int TPC = TT >= 128 ? 1 : 128 / TT;  // tiles per stage
   static constexpr int THREADS = TPC * TT;
   static constexpr int KB = NZ * 128;            // bytes of a spectrum tile
-  static constexpr int LB = NZ * 64;             // bytes of an LD tile (M values of T per row)
+  static constexpr int LB = NZ * M * (int)sizeof(T);  // bytes of an LD tile
 #ifndef PF_ZSTAGES
-#define PF_ZSTAGES 2
+#define PF_ZSTAGES 3
 #endif
   static constexpr int STAGES = PF_ZSTAGES;
-  static constexpr int SMEM = STAGES * TPC * (KB + LB) + 1024;  // + alignment of the 1024-byte swizzle atom
-  // CTAs per SM that the shared memory allows (at most 4): the register budget follows from it
+  static constexpr int SMEM = STAGES * TPC * (KB + LB) + 1024;  // + alignment of the buffers
+  // CTAs per SM that the shared memory allows (at most PF_ZMINB): the register budget follows
 #ifndef PF_ZMINB
-#define PF_ZMINB 3
+#define PF_ZMINB 4
 #endif
   static constexpr int MINB =
       (200 * 1024 / SMEM) < 1 ? 1 : ((200 * 1024 / SMEM) > PF_ZMINB ? PF_ZMINB : (200 * 1024 / SMEM));
-  // group -> pencil stride (a bank-conflict count under the swizzle picked 5 for 4-thread groups)
-  static constexpr int PSTRIDE = G == 4 ? 5 : 1;
 };
 
-// Row order of the intermediate passes (a bijection on [0, NZ) that only permutes the low
-// three bits, i.e. the 16-byte chunk a row's element lands in under the 128-byte swizzle).
-template <int NZ>
-__device__ __forceinline__ int zrow_perm(int i) {
-  if constexpr (NZ == 128 || NZ == 96) return i ^ (((i >> 3) ^ (i >> 6)) & 7);
-  else if constexpr (NZ == 64 || NZ == 32) return i ^ ((i >> 3) & 7);
-  else if constexpr (NZ == 256) return swz(i);
-  else return i;
-}
-
-// Element (row z, pencil m) of a spectrum tile under the 128-byte swizzle: the 16-byte chunk
-// index of the 128-byte row is XORed with z mod 8 (the buffer is 1024-byte aligned).
-template <typename T>
-__device__ __forceinline__ int ktile_index(int z, int m) {
-  constexpr int E = (int)sizeof(Cx<T>);
-  const int b = m * E;
-  return (z * 128 + ((((b >> 4) ^ (z & 7)) << 4) | (b & 15))) / E;
-}
-// Element (row z, pencil m) of an LD tile under the 64-byte swizzle: the chunk index of the
-// 64-byte row is XORed with (z / 2) mod 4 (the buffer is 512-byte aligned).
-template <typename T>
-__device__ __forceinline__ int ltile_index(int z, int m) {
-  const int b = m * (int)sizeof(T);
-  return (z * 64 + ((((b >> 4) ^ ((z >> 1) & 3)) << 4) | (b & 15))) / (int)sizeof(T);
-}
-
+// Passes p in [P0, P1) of the transform of one pencil, in place on its tile column (element z
+// at kt[z * M]), between block barriers.
 template <typename T, bool INV, int N, int O, int P0, int P1>
-__device__ __forceinline__ void ztile_passes(Cx<T>* kt, int m, int g, const Cx<T>* tw, bool active) {
+__device__ __forceinline__ void ztile_passes(Cx<T>* kt, int g, const Cx<T>* tw, bool active) {
+  constexpr int M = ZPipe<T, N>::M;
   if constexpr (P0 < P1) {
     using PS = PassOf<T, INV, N, O, P0>;
     Cx<T> v[PS::BPT][Order<N, O>::radix(P0)];
     if (active) {
-      PS::load(v, g, [&](int i) { return kt[ktile_index<T>(zrow_perm<N>(i), m)]; });
+      PS::load(v, g, [&](int i) { return kt[i * M]; });
       PS::compute(v, g, tw + Order<N, O>::tw_offset(P0));
     }
-    __syncwarp();
-    if (active) PS::store(v, g, [&](int i, const Cx<T>& x) { kt[ktile_index<T>(zrow_perm<N>(i), m)] = x; });
-    __syncwarp();
-    ztile_passes<T, INV, N, O, P0 + 1, P1>(kt, m, g, tw, active);
+    __syncthreads();
+    if (active) PS::store(v, g, [&](int i, const Cx<T>& x) { kt[i * M] = x; });
+    __syncthreads();
+    ztile_passes<T, INV, N, O, P0 + 1, P1>(kt, g, tw, active);
   }
 }
 
-// Forward z transform (order B) of pencil m of a tile, ending in registers at the B -> A join.
+// Forward z transform (order B) of one pencil (kt = tile + m), ending in registers at the
+// B -> A join.
 template <typename T, int NZ>
-__device__ __forceinline__ void ztile_forward(Cx<T>* kt, int m, int g, const Cx<T>* twb, BARegs<T, NZ>& w,
-                                              bool active) {
+__device__ __forceinline__ void ztile_forward(Cx<T>* kt, int g, const Cx<T>* twb, BARegs<T, NZ>& w, bool active) {
   constexpr int P = Order<NZ, 1>::P;
+  constexpr int M = ZPipe<T, NZ>::M;
   using F0 = PassOf<T, false, NZ, 1, 0>;
   if constexpr (P == 1) {
     if (active) {
-      F0::load(w.v, g, [&](int i) { return kt[ktile_index<T>(i, m)]; });
+      F0::load(w.v, g, [&](int i) { return kt[i * M]; });
       F0::compute(w.v, g, twb);
     }
   } else {
     Cx<T> v[F0::BPT][Order<NZ, 1>::radix(0)];
     if (active) {
-      F0::load(v, g, [&](int i) { return kt[ktile_index<T>(i, m)]; });
+      F0::load(v, g, [&](int i) { return kt[i * M]; });
       F0::compute(v, g, twb);
     }
-    __syncwarp();
-    if (active) F0::store(v, g, [&](int i, const Cx<T>& x) { kt[ktile_index<T>(zrow_perm<NZ>(i), m)] = x; });
-    __syncwarp();
-    ztile_passes<T, false, NZ, 1, 1, P - 1>(kt, m, g, twb, active);
+    __syncthreads();
+    if (active) F0::store(v, g, [&](int i, const Cx<T>& x) { kt[i * M] = x; });
+    __syncthreads();
+    ztile_passes<T, false, NZ, 1, 1, P - 1>(kt, g, twb, active);
     using FL = PassOf<T, false, NZ, 1, P - 1>;
     if (active) {
-      FL::load(w.v, g, [&](int i) { return kt[ktile_index<T>(zrow_perm<NZ>(i), m)]; });
+      FL::load(w.v, g, [&](int i) { return kt[i * M]; });
       FL::compute(w.v, g, twb + Order<NZ, 1>::tw_offset(P - 1));
     }
   }
-  __syncwarp();
+  __syncthreads();
 }
 
 // Inverse z transform (order A) from registers at the join back into the tile, natural rows.
 template <typename T, int NZ>
-__device__ __forceinline__ void ztile_inverse(Cx<T>* kt, int m, int g, const Cx<T>* twa, BARegs<T, NZ>& w,
-                                              bool active) {
+__device__ __forceinline__ void ztile_inverse(Cx<T>* kt, int g, const Cx<T>* twa, BARegs<T, NZ>& w, bool active) {
   constexpr int P = Order<NZ, 0>::P;
+  constexpr int M = ZPipe<T, NZ>::M;
   using I0 = PassOf<T, true, NZ, 0, 0>;
   if constexpr (P == 1) {
     if (active) {
       I0::compute(w.v, g, twa);
-      I0::store(w.v, g, [&](int i, const Cx<T>& x) { kt[ktile_index<T>(i, m)] = x; });
+      I0::store(w.v, g, [&](int i, const Cx<T>& x) { kt[i * M] = x; });
     }
   } else {
     if (active) {
       I0::compute(w.v, g, twa);
-      I0::store(w.v, g, [&](int i, const Cx<T>& x) { kt[ktile_index<T>(zrow_perm<NZ>(i), m)] = x; });
+      I0::store(w.v, g, [&](int i, const Cx<T>& x) { kt[i * M] = x; });
     }
-    __syncwarp();
-    ztile_passes<T, true, NZ, 0, 1, P - 1>(kt, m, g, twa, active);
+    __syncthreads();
+    ztile_passes<T, true, NZ, 0, 1, P - 1>(kt, g, twa, active);
     using IL = PassOf<T, true, NZ, 0, P - 1>;
     Cx<T> v[IL::BPT][Order<NZ, 0>::radix(P - 1)];
     if (active) {
-      IL::load(v, g, [&](int i) { return kt[ktile_index<T>(zrow_perm<NZ>(i), m)]; });
+      IL::load(v, g, [&](int i) { return kt[i * M]; });
       IL::compute(v, g, twa + Order<NZ, 0>::tw_offset(P - 1));
     }
-    __syncwarp();
-    if (active) IL::store(v, g, [&](int i, const Cx<T>& x) { kt[ktile_index<T>(i, m)] = x; });
+    __syncthreads();
+    if (active) IL::store(v, g, [&](int i, const Cx<T>& x) { kt[i * M] = x; });
   }
 }
 
@@ -797,7 +776,7 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
   if (threadIdx.x == 0)
     for (int k = 0; k < S - 1 && k < nk; ++k) issue(k);
   const int slot = threadIdx.x / Z::TT, lt = threadIdx.x % Z::TT;
-  const int m = ((lt / G) * Z::PSTRIDE) % Z::M, g = lt % G;
+  const int m = lt % Z::M, g = lt / Z::M;  // pencil-major lanes
   const Cx<T>* twb = twz + Order<NZ, 0>::TW_SIZE;
   int waited = 0;  // rounds whose stage completed
   bool ok = true;
@@ -810,12 +789,18 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
       break;
     }
     waited = k + 1;
+    // refill the stage that round k-1 used with round k + S - 1 now, so that its copies overlap
+    // this round's transforms (the store of round k-1 must have finished reading that stage)
+    if (threadIdx.x == 0 && k + S - 1 < nk) {
+      bulk_wait_read<0>();
+      issue(k + S - 1);
+    }
     const int tile = r * TPC + slot;
     const bool active = tile < ntiles;
-    Cx<T>* kt = ktiles + (size_t)(s * TPC + slot) * (Z::KB / Z::E);
-    const T* ltl = ltiles + (size_t)(s * TPC + slot) * (Z::LB / sizeof(T));
+    Cx<T>* kt = ktiles + (size_t)(s * TPC + slot) * (Z::KB / Z::E) + m;
+    const T* ltl = ltiles + (size_t)(s * TPC + slot) * (Z::LB / sizeof(T)) + m;
     BARegs<T, NZ> w;
-    ztile_forward<T, NZ>(kt, m, g, twb, w, active);
+    ztile_forward<T, NZ>(kt, g, twb, w, active);
     if (csc && r == 0 && threadIdx.x == 0) {
       // tile 0, pencil 0, position 0: the (0, 0, 0) coefficient = grid sum of LW * q_t
       const T c = rescale_factor<T>(w.v[0][0].x, ng);
@@ -827,12 +812,12 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
       for (int b = 0; b < JoinBA<NZ>::BPT; ++b)
 #pragma unroll
         for (int tt = 0; tt < JoinBA<NZ>::R; ++tt) {
-          const T f = ltl[ltile_index<T>(JoinBA<NZ>::pos(g, b, tt), m)];
+          const T f = ltl[JoinBA<NZ>::pos(g, b, tt) * Z::M];
           w.v[b][tt] = cx<T>(w.v[b][tt].x * f, w.v[b][tt].y * f);
         }
     }
     if (k == nk - 1) grid_dep_launch();  // last round: the next plane pass may be scheduled
-    ztile_inverse<T, NZ>(kt, m, g, twz, w, active);
+    ztile_inverse<T, NZ>(kt, g, twz, w, active);
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -840,10 +825,6 @@ __global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
       for (int j = 0; j < nt; ++j)
         tma_store_2d(&kmap, (r * TPC + j) * 16, 0, ktiles + (size_t)(s * TPC + j) * (Z::KB / Z::E));
       bulk_commit();
-      if (k + S - 1 < nk) {
-        bulk_wait_read<1>();  // the store of round k-1 has left stage (k-1) % S
-        issue(k + S - 1);
-      }
     }
   }
   if (threadIdx.x == 0) {
@@ -1187,8 +1168,8 @@ static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
 }
 
 // TMA views of a chain's half-spectrum scratch (rows of Nkp complex values, one per kz, as
-// 8-byte units; boxes of 128 bytes x Nz rows, 128-byte swizzle) and of an LD array (rows of
-// Nkp values of T; boxes of 64 bytes x Nz rows, 64-byte swizzle).
+// 8-byte units; boxes of 128 bytes x Nz rows) and of an LD array (rows of Nkp values of T;
+// boxes of M values x Nz rows), both unswizzled: the pencil pass reads whole rows per half warp.
 template <typename T>
 static void make_zmaps(CUtensorMap* km, CUtensorMap* lm, const Cx<T>* kbuf, const T* ld, int nkp, int nz) {
   auto enc = tmap_encoder();
@@ -1202,16 +1183,16 @@ static void make_zmaps(CUtensorMap* km, CUtensorMap* lm, const Cx<T>* kbuf, cons
     const cuuint64_t str[1] = {(cuuint64_t)nkp * sizeof(Cx<T>)};
     const cuuint32_t box[2] = {16, (cuuint32_t)nz};
     if (enc(km, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<Cx<T>*>(kbuf), dim, str, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       throw DeviceError("cuTensorMapEncodeTiled failed for a half-spectrum scratch");
   }
   {
     const cuuint64_t dim[2] = {(cuuint64_t)nkp, (cuuint64_t)nz};
     const cuuint64_t str[1] = {(cuuint64_t)nkp * sizeof(T)};
-    const cuuint32_t box[2] = {(cuuint32_t)(64 / sizeof(T)), (cuuint32_t)nz};
+    const cuuint32_t box[2] = {(cuuint32_t)z_tile_pencils<T>(), (cuuint32_t)nz};
     if (enc(lm, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2,
-            const_cast<T*>(ld), dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+            const_cast<T*>(ld), dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       throw DeviceError("cuTensorMapEncodeTiled failed for a bond operator");
   }
