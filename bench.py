@@ -237,19 +237,19 @@ def run_gpu(args):
     alg_bytes = 3 * 4 * ng  # read q_s (f32), read LW (f32), write q_{s+1} (f32)
     achieved = alg_bytes / (mde_step_us * 1e-6) / 1e9
     # DRAM bytes of one contour step of one chain at 128^3 (xy_step + z_pipe launches) from an
-    # ncu capture of the large blend with Ns = 20 (profile_mde.py --blend): reads 16.96 MB +
-    # 12.82 MB, writes 0 (absorbed by L2 within the launch); cold caches.
-    traffic = 29.78e6 if n == 128 else None
+    # ncu capture of the large blend with Ns = 20 (bench.py --mode profile): reads 16.96 MB +
+    # 12.81 MB, writes 0 (absorbed by L2 within the launch); cold caches.
+    traffic = 29.77e6 if n == 128 else None
     roofline = {"bound": "hbm", "kernel": "MDE contour step (xy_step_kernel<float,128,128> + z_pipe_kernel<float,128>)",
                 "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
                 "avg_step_us": mde_step_us}
-    # The step is issue bound before it is HBM bound: ncu counts 5.59e6 + 3.02e6 warp instructions
-    # for one chain step at 128^3 (plane + pencil pass); 152 SMs x 4 schedulers issue at most one
-    # warp instruction per cycle each at the sampled SM clock.
+    # The step is issue bound before it is HBM bound: ncu counts 4.91e6 + 1.66e6 warp instructions
+    # for one chain step at 128^3 (plane + pencil pass, same capture); 152 SMs x 4 schedulers issue
+    # at most one warp instruction per cycle each at the sampled SM clock.
     issue = None
     if n == 128:
-        winst = 5.59e6 + 3.02e6
+        winst = 4.91e6 + 1.66e6
         mhz = (clk or {}).get("sm_mhz") or 2070.0
         floor_us = winst / (152 * 4 * mhz * 1e6) * 1e6
         issue = {"warp_instructions_per_step": winst, "floor_us": floor_us, "frac": floor_us / mde_step_us}
