@@ -201,6 +201,15 @@ int pf_set_density_cotangent(pf_system* sys, int mid, const double* rho_bar);
  * read the stored histories. */
 int pf_set_adjoint_checkpoints(pf_system* sys, int every);
 int pf_density_pullback(pf_system* sys, double* cell_bar, int ncell, double* nref_bar, int nnref);
+/* Gradient of free_energy(sys) (src/system/system.jl:402-433, with the translational term as the
+ * reference computes it, mu = phi) at the current fields and cell, with respect to the fields
+ * (read as pf_get_grid(..., PF_FIELD_COTANGENT, mid, out)), the cell parameters (cell_bar), the
+ * block lengths Nref_b (nref_bar, as for pf_density_pullback), the Flory chi of every pair in
+ * ascending (id_a, id_b) order, id_a < id_b (chi_bar), and the Edwards u of every monomer that has
+ * one, in ascending id order (u_bar); *fhelm receives free_energy.  Solves density! first and
+ * replaces the density cotangent of pf_set_density_cotangent.  Canonical ensemble, RK2. */
+int pf_free_energy_pullback(pf_system* sys, double* cell_bar, int ncell, double* nref_bar, int nnref, double* chi_bar,
+                            int nchi, double* u_bar, int nu, double* fhelm);
 
 /* Many independent scft! runs (a phase-diagram sweep: src/simulate.jl:60-148 once per
  * FieldSystem) driven together: nthreads host threads (0: min(n, 32)) take the systems in

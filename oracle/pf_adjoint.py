@@ -1,4 +1,5 @@
-"""FP64 CPU reference gradient of the density map w -> rho (the pullback of density!).
+"""FP64 CPU reference gradients of the density map w -> rho (the pullback of density!) and of
+free_energy at fixed fields.
 
 TEST INFRASTRUCTURE ONLY, like pf_oracle.py: the checker the GPU adjoint is compared
 against.  PolyFields.jl has no derivative code; this module differentiates the oracle's
@@ -152,6 +153,42 @@ def density_pullback(sys, rho_bar: Dict[int, np.ndarray]) -> Dict:
         # ds_b = Nref_b / Ns_b and rho ~ 1 / Nref with Nref = sum_b Nref_b
         grads["Nref_block"].append([dds[i] / (bounds[i][1] - bounds[i][0]) - S / Nref for i in range(nb)])
     return grads
+
+
+def free_energy_pullback(sys) -> Dict:
+    """d free_energy / d(w, cell, Nref_b, chi, u) at fixed fields, for a canonical system that
+    has run density_update().  free_energy (src/system/system.jl:402-433, as restated in
+    pf_oracle: translational term with mu = phi, -<rho w>, interaction energies) depends on w
+    directly through -sum rho w / Ng and through rho(w); on chi and u only through the
+    interaction energies (src/interactions/flory.jl:39-59, edwards.jl:34-60); on the block
+    lengths through rho and through the translational term phi (phi - 1) / Nref."""
+    ng = sys.ngrid
+    vol = {m: sys.monomers[m].vol for m in sys.monomers}
+    rho = sys.density
+    rbar = {m: -sys.fields[m] / ng for m in sys.monomers}
+    chi_bar, u_bar = {}, {}
+    for itx in sys.interactions:
+        if isinstance(itx, O.FloryInteraction):
+            for (a, b), chi in itx.chis.items():
+                if a in sys.monomers and b in sys.monomers:
+                    rbar[a] = rbar[a] + chi * rho[b] / (vol[a] * vol[b]) / ng
+                    rbar[b] = rbar[b] + chi * rho[a] / (vol[a] * vol[b]) / ng
+                    chi_bar[(a, b)] = float(np.sum(rho[a] * rho[b])) / (vol[a] * vol[b]) / ng
+        elif isinstance(itx, O.EdwardsInteraction):
+            for m, u in itx.uvals.items():
+                if m in sys.monomers:
+                    rbar[m] = rbar[m] + u * rho[m] / vol[m] ** 2 / ng
+                    u_bar[m] = float(np.sum(0.5 * (rho[m] / vol[m]) ** 2)) / ng
+    g = density_pullback(sys, rbar)
+    for m in sys.monomers:
+        g["w"][m] = g["w"][m] - rho[m] / ng
+    g["chi"] = chi_bar
+    g["u"] = u_bar
+    for isp, sp in enumerate(sys.species):
+        phi = sys.phi_species[isp]
+        if isinstance(sp, O.Multiblock) and phi > 1e-8:
+            g["Nref_block"][isp] = [v - phi * (phi - 1.0) / sp.Nref ** 2 for v in g["Nref_block"][isp]]
+    return g
 
 
 def density_loss(sys, mid: int, target: np.ndarray):

@@ -133,6 +133,30 @@ void launch_adj_point(double* wbar, const double* rho, const double* rb, const d
   count_launches(1);
 }
 
+// dL/drho_a of L = free_energy at fixed fields (system.jl:402-433 with flory.jl:39-59 and
+// edwards.jl:34-60): (-w_a + sum_b chi_ab rho_b / (v_a v_b)) / Ng; the diagonal of chi holds
+// the Edwards u (energy (u/2) (rho/v)^2, derivative u rho / v^2).
+static __global__ void fhelm_cotangent_kernel(double* __restrict__ rbar, const double* __restrict__ w,
+                                              const double* __restrict__ rho, MonomerSet ms, long ng) {
+  const double inv = 1.0 / (double)ng;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < ng; i += (long)gridDim.x * blockDim.x) {
+    for (int a = 0; a < ms.nmon; ++a) {
+      double s = -w[(long)a * ng + i];
+      for (int b = 0; b < ms.nmon; ++b) {
+        const double c = ms.chi[a * kMaxMon + b];
+        if (c != 0.0) s += c * rho[(long)b * ng + i] / (ms.vol[a] * ms.vol[b]);
+      }
+      rbar[(long)a * ng + i] = s * inv;
+    }
+  }
+}
+
+void launch_fhelm_cotangent(double* rbar, const double* w, const double* rho, const MonomerSet& ms, long ng,
+                            cudaStream_t st) {
+  fhelm_cotangent_kernel<<<adj_blocks(ng), 256, 0, st>>>(rbar, w, rho, ms, ng);
+  count_launches(1);
+}
+
 void launch_daxpy(double* y, const double* x, double a, long n, cudaStream_t st) {
   daxpy_kernel<<<adj_blocks(n), 256, 0, st>>>(y, x, a, n);
   count_launches(1);

@@ -1712,11 +1712,11 @@ struct System {
   // forward chain t = Ns-1 .. 0 and backward chain s = 1 .. Ns, one contour step at a time
   // through the forward kernels (the block operator is symmetric).
   template <typename T>
-  void pullback_t(int p, std::vector<double>& cell_bar, std::vector<double>& nref_bar) {
+  void pullback_t(int p, std::vector<double>& cell_bar, std::vector<double>& nref_bar, bool recompute = true) {
     require_ready();
     if (mde != 0) throw PFError(E_UNSUPPORTED, "the pullback differentiates the RK2 propagator");
     if (ensemble != 0) throw PFError(E_UNSUPPORTED, "the pullback differentiates the canonical ensemble");
-    density_t<T>(p);
+    if (recompute || last_prec != p) density_t<T>(p);
     fetch_Q();
     const int npr = cell.np(), nw = npr + 1;
     const CellGeom g = geom();
@@ -1945,9 +1945,61 @@ struct System {
     PF_CU(cudaStreamSynchronize(st));
     check_pipe(p);
   }
-  void pullback(std::vector<double>& cell_bar, std::vector<double>& nref_bar) {
-    if (prec == 0) pullback_t<double>(0, cell_bar, nref_bar);
-    else pullback_t<float>(1, cell_bar, nref_bar);
+  void pullback(std::vector<double>& cell_bar, std::vector<double>& nref_bar, bool recompute = true) {
+    if (prec == 0) pullback_t<double>(0, cell_bar, nref_bar, recompute);
+    else pullback_t<float>(1, cell_bar, nref_bar, recompute);
+  }
+
+  // Gradient of free_energy (system.jl:402-433) at the current fields and cell: density! is
+  // solved, dL/drho = (-w + sum chi rho / (v v)) / Ng is set as the density cotangent (it
+  // replaces one set by pf_set_density_cotangent), the density pullback gives the chain
+  // dependence, and the direct terms are added: -rho / Ng to dL/dw, <rho_a rho_b> / (v_a v_b)
+  // to dL/dchi_ab (Flory pairs in ascending id order), <(rho/v)^2> / 2 to dL/du (Edwards
+  // monomers in ascending id order), and -phi (phi - 1) / Nref^2 (the translational term with
+  // mu = phi, as the reference computes it) to dL/dNref of every block.  Returns free_energy.
+  double fhelm_pullback(std::vector<double>& cell_bar, std::vector<double>& nref_bar, std::vector<double>& chi_bar,
+                        std::vector<double>& u_bar) {
+    require_ready();
+    if (ensemble != 0) throw PFError(E_UNSUPPORTED, "the pullback differentiates the canonical ensemble");
+    density();
+    fetch_Q();
+    double ferr = 0.0, fhelm = 0.0;
+    stats(ferr, fhelm);
+    launch_fhelm_cotangent(rbar.as<double>(), w.as<double>(), rho.as<double>(), monomer_set(), ng, st);
+    check_launch();
+    pullback(cell_bar, nref_bar, false);
+    launch_daxpy(wbar.as<double>(), rho.as<double>(), -1.0 / (double)ng, (long)nmon() * ng, st);
+    DevBuf dp, dd;
+    dp.alloc(sizeof(double) * kRedBlocks);
+    dd.alloc(sizeof(double));
+    auto dot = [&](const double* a, const double* b) {
+      launch_ddot(a, b, ng, dp.as<double>(), dd.as<double>(), st);
+      double v = 0.0;
+      PF_CU(cudaMemcpyAsync(&v, dd.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+      PF_CU(cudaStreamSynchronize(st));
+      return v;
+    };
+    chi_bar.clear();
+    for (auto& kv : chis) {
+      const int a = kv.first.first, b = kv.first.second;
+      const double va = monomers.at(a).first, vb = monomers.at(b).first;
+      chi_bar.push_back(dot(grid_ptr(rho, a), grid_ptr(rho, b)) / (va * vb * (double)ng));
+    }
+    u_bar.clear();
+    for (auto& kv : edwards) {
+      const double v = monomers.at(kv.first).first;
+      const double* r = grid_ptr(rho, kv.first);
+      u_bar.push_back(0.5 * dot(r, r) / (v * v * (double)ng));
+    }
+    size_t k = 0;
+    for (auto& sp : species) {
+      if (sp->kind != 0) continue;
+      const double phi = sp->phi, t = phi > 1e-8 ? -phi * (phi - 1.0) / (sp->Nref * sp->Nref) : 0.0;
+      for (int b = 0; b < sp->nblocks() && k < nref_bar.size(); ++b) nref_bar[k++] += t;
+    }
+    check_launch();
+    PF_CU(cudaStreamSynchronize(st));
+    return fhelm;
   }
 
   // ---------------------------------------------------------------- scft! (simulate.jl:60-148)
@@ -2519,6 +2571,23 @@ int pf_density_pullback(pf_system* sys, double* cell_bar, int ncell, double* nre
       for (int i = 0; i < std::min(ncell, (int)cb.size()); ++i) cell_bar[i] = cb[i];
     if (nref_bar)
       for (int i = 0; i < std::min(nnref, (int)nb.size()); ++i) nref_bar[i] = nb[i];
+  });
+}
+
+int pf_free_energy_pullback(pf_system* sys, double* cell_bar, int ncell, double* nref_bar, int nnref, double* chi_bar,
+                            int nchi, double* u_bar, int nu, double* fhelm) {
+  return guard(sys, [&](pf::System& s) {
+    std::vector<double> cb, nb, xb, ub;
+    const double f = s.fhelm_pullback(cb, nb, xb, ub);
+    if (fhelm) *fhelm = f;
+    if (cell_bar)
+      for (int i = 0; i < std::min(ncell, (int)cb.size()); ++i) cell_bar[i] = cb[i];
+    if (nref_bar)
+      for (int i = 0; i < std::min(nnref, (int)nb.size()); ++i) nref_bar[i] = nb[i];
+    if (chi_bar)
+      for (int i = 0; i < std::min(nchi, (int)xb.size()); ++i) chi_bar[i] = xb[i];
+    if (u_bar)
+      for (int i = 0; i < std::min(nu, (int)ub.size()); ++i) u_bar[i] = ub[i];
   });
 }
 

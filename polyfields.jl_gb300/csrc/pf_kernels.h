@@ -162,6 +162,10 @@ void launch_adj_accum(double* acc, const double* part, int nparts, int nw, const
 // Point species: wbar += -vol * rho * rb + S * vol * exp(-vol * w) / (Ng * Q)
 void launch_adj_point(double* wbar, const double* rho, const double* rb, const double* w, double vol, double S,
                       double ngQ, long n, cudaStream_t st);
+// dL/drho of L = free_energy at fixed fields, every monomer: (-w_a + sum_b chi_ab rho_b / (v_a v_b)) / Ng
+struct MonomerSet;
+void launch_fhelm_cotangent(double* rbar, const double* w, const double* rho, const MonomerSet& ms, long ng,
+                            cudaStream_t st);
 // y += a * x (float64 grids)
 void launch_daxpy(double* y, const double* x, double a, long n, cudaStream_t st);
 // sum_x a_x * b_x into *out (device), float64, deterministic

@@ -238,6 +238,40 @@ function ChainRulesCore.rrule(::typeof(density), sys::FieldSystem, w::Dict{Int,A
     return rho, density_pullback
 end
 
+# free_energy(sys, w) as a differentiable function (pf_free_energy_pullback): the pullback gives
+# dF/dw per monomer and, as the system's tangent, dF/dtheta (cell), dF/dNref_b (blocks), dF/dchi
+# (Flory pairs in ascending id order) and dF/du (Edwards monomers in ascending id order).
+function ChainRulesCore.rrule(::typeof(PolyFields.free_energy), sys::FieldSystem, w::Dict{Int,Array{Float64,3}};
+                              precision::Integer = 0)
+    h = gpu_system(sys; precision)
+    for (mid, wm) in w
+        GC.@preserve wm check(h, ccall((:pf_set_field, lib), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}), h, mid, wm))
+    end
+    np = length(sys.cell.params)
+    nblk = sum((length(sp.N_block) for sp in sys.species if sp isa Multiblock); init = 0)
+    pairs = sort(unique([p for itx in sys.interactions if itx isa FloryInteraction for p in keys(itx.chis)]))
+    umids = sort(unique([m for itx in sys.interactions if itx isa EdwardsInteraction for m in keys(itx.uvals)]))
+    cell_bar, nref_bar = zeros(max(np, 1)), zeros(max(nblk, 1))
+    chi_bar, u_bar, f = zeros(max(length(pairs), 1)), zeros(max(length(umids), 1)), Ref(0.0)
+    check(h, ccall((:pf_free_energy_pullback, lib), Cint,
+                   (Ptr{Cvoid}, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ref{Cdouble}),
+                   h, cell_bar, np, nref_bar, nblk, chi_bar, length(pairs), u_bar, length(umids), f))
+    w_bar = Dict(mid => similar(wm) for (mid, wm) in w)
+    for (mid, g) in w_bar
+        GC.@preserve g check(h, ccall((:pf_get_grid, lib), Cint, (Ptr{Cvoid}, Cint, Cint, Ptr{Cdouble}),
+                                      h, PF_FIELD_COTANGENT, mid, g))
+    end
+    ccall((:pf_system_destroy, lib), Cint, (Ptr{Cvoid},), h)
+    function free_energy_pullback(fbar)
+        s = unthunk(fbar)
+        tangent = Tangent{typeof(sys)}(; cell = s .* cell_bar[1:np], Nref_block = s .* nref_bar[1:nblk],
+                                       chi = Dict(p => s * chi_bar[i] for (i, p) in enumerate(pairs)),
+                                       u = Dict(m => s * u_bar[i] for (i, m) in enumerate(umids)))
+        return NoTangent(), tangent, Dict(mid => s .* g for (mid, g) in w_bar)
+    end
+    return f[], free_energy_pullback
+end
+
 # Contour steps of one chain on device buffers the caller owns (CuArray pointers), with no
 # device allocation by the engine (pf_propagate_noalloc); `stream` is a CUDA stream handle
 # (C_NULL: default stream).  Returns once the work is queued; call

@@ -80,6 +80,7 @@ SIGNATURES = {
     "pf_set_density_cotangent": (_c_int, [_vp, _c_int, _dptr]),
     "pf_set_adjoint_checkpoints": (_c_int, [_vp, _c_int]),
     "pf_density_pullback": (_c_int, [_vp, _dptr, _c_int, _dptr, _c_int]),
+    "pf_free_energy_pullback": (_c_int, [_vp, _dptr, _c_int, _dptr, _c_int, _dptr, _c_int, _dptr, _c_int, _dptr]),
     "pf_scft_batch": (_c_int, [ctypes.POINTER(_vp), _c_int, ctypes.POINTER(ScftOptions), _c_int,
                                ctypes.POINTER(ScftResults), ctypes.POINTER(_c_int), _c_int]),
     "pf_propagate": (_c_int, [_vp, _dptr, _c_double, _c_double, _c_double, _dptr, _dptr, _c_int]),

@@ -423,6 +423,36 @@ class FieldSystem:
                 out["chi"][pair] = 0.0
         return out
 
+    def free_energy_pullback(self) -> Dict:
+        """Gradient of free_energy (src/system/system.jl:402-433) at the current fields and cell:
+        {"fhelm": value, "w": {mid: dF/dw_mid}, "cell": dF/dtheta, "Nref_block": [per species,
+        dF/dNref_b of each block (empty for point species)], "chi": {(a, b): dF/dchi_ab},
+        "u": {mid: dF/du_mid}}.  Solves density! first; replaces the density cotangent."""
+        lib = L.load()
+        npr = len(self.cell.params)
+        nblk = [len(sp.N_block) if isinstance(sp, Multiblock) else 0 for sp in self.species]
+        pairs = sorted({pair for itx in self.interactions for pair in getattr(itx, "chis", {})})
+        umids = sorted({m for itx in self.interactions for m in getattr(itx, "uvals", {})})
+        cell_bar = np.zeros(max(1, npr))
+        nref = np.zeros(max(1, sum(nblk)))
+        chi = np.zeros(max(1, len(pairs)))
+        ub = np.zeros(max(1, len(umids)))
+        f = ctypes.c_double()
+        L.check(lib.pf_free_energy_pullback(self._h, L.dptr(cell_bar), npr, L.dptr(nref), sum(nblk), L.dptr(chi),
+                                            len(pairs), L.dptr(ub), len(umids), ctypes.byref(f)), self._h)
+        out = {"fhelm": f.value, "w": {}, "cell": cell_bar[:npr].copy(), "Nref_block": [],
+               "chi": {pair: float(chi[i]) for i, pair in enumerate(pairs)},
+               "u": {m: float(ub[i]) for i, m in enumerate(umids)}}
+        for mid in self.monomers:
+            g = np.empty(self.shape)
+            L.check(lib.pf_get_grid(self._h, L.PF_FIELD_COTANGENT, mid, L.dptr(g)), self._h)
+            out["w"][mid] = g
+        k = 0
+        for n in nblk:
+            out["Nref_block"].append(list(nref[k:k + n]))
+            k += n
+        return out
+
     def set_wait_limit(self, seconds: float) -> None:
         """Time limit of the 3D pencil passes' bounded waits for their TMA copies (default 1 s).
         A wait that runs out invalidates the solve: the next call that reads results raises

@@ -91,3 +91,50 @@ def test_simpson_weights_match_the_reference_sum():
         if n % 2 == 0:  # exact for cubics on an even number of intervals
             assert np.dot(w, x ** 3) / 3.0 / n == pytest.approx(0.25, rel=1e-12)
         assert w[0] == 1.0 and w[n] == 1.0
+
+
+FE_CASES = [
+    ("hex2d", (16, 16, 1), "hexagonal", [6.0], False),
+    ("cubic3d", (8, 8, 8), "cubic", [5.0], False),
+    ("blend2d", (16, 8, 1), "rectangular", [6.0, 4.0], True),
+]
+
+
+@pytest.mark.parametrize("name,dims,crystal,params,blend", FE_CASES, ids=[c[0] for c in FE_CASES])
+def test_free_energy_pullback_matches_central_differences(name, dims, crystal, params, blend):
+    """d free_energy / d(w, cell, N_A, chi) at fixed fields (src/system/system.jl:402-433) against
+    central differences of the oracle's free_energy."""
+    shape = (dims[2], dims[1], dims[0])
+    rng = np.random.default_rng(17)
+    mids = [1, 2, 3] if blend else [1, 2]
+    fields = {m: 0.4 * rng.standard_normal(shape) for m in mids}
+    NA, NB = 35.0, 65.0
+
+    def fhelm(fields=fields, params=params, NA=NA, chi=0.2):
+        s = build(dims, crystal, params, NA, NB, fields, blend=blend)
+        s.interactions[0].chis[(1, 2)] = chi
+        return s.free_energy()
+
+    sys = build(dims, crystal, params, NA, NB, fields, blend=blend)
+    g = AD.free_energy_pullback(sys)
+    h = 1e-5
+
+    def cd(f):
+        return (f(+h) - f(-h)) / (2 * h)
+
+    for m in mids:
+        for idx in [(0, 0, 3), (shape[0] - 1, shape[1] - 1, shape[2] - 2)]:
+            def fw(d, m=m, idx=idx):
+                f2 = {k: v.copy() for k, v in fields.items()}
+                f2[m][idx] += d
+                return fhelm(fields=f2)
+            assert g["w"][m][idx] == pytest.approx(cd(fw), rel=1e-6, abs=1e-12), (m, idx)
+    for p in range(len(params)):
+        def fc(d, p=p):
+            q = list(params)
+            q[p] += d
+            return fhelm(params=q)
+        assert g["cell"][p] == pytest.approx(cd(fc), rel=1e-6, abs=1e-12)
+    assert g["Nref_block"][0][0] == pytest.approx(cd(lambda d: fhelm(NA=NA + d)), rel=1e-6, abs=1e-12)
+    assert g["chi"][(1, 2)] == pytest.approx(cd(lambda d: fhelm(chi=0.2 + d)), rel=1e-7)
+    assert g["chi"][(1, 2)] != 0.0
