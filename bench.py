@@ -231,6 +231,7 @@ def run_gpu(args):
     mde_step_us = 1000.0 * prop_step_ms / nmde
     ferr = sysm.field_error()
     fhelm = sysm.free_energy()
+    sysm_schedule = sysm.pencil_schedule()
 
     # ---- roofline of the dominant kernel pair (one MDE contour step: xy_step + z_pipe)
     peak, peak_kind = measured_peaks()
@@ -302,7 +303,8 @@ def run_gpu(args):
             "density_ms_per_iter": dens_ms / args.steps, "host_ms_per_step": 1000.0 * t_host / args.steps,
             "fp64": fp64, "mixed_vs_fp64_iter_speedup": (value / fp64["iters_per_s"]) if fp64 else None,
             "ferr": ferr, "fhelm": fhelm, "fhelm_initial": fhelm_initial, "roofline": roofline, "issue_roofline": issue, "e2e": e2e,
-            "gpu_launches": int(launches),
+            "gpu_launches": int(launches), "pencil_schedule": dict(zip(("stages", "rounds", "autotuned"),
+                                                                       sysm_schedule)),
             "clocks": clk, "cpu_baseline": cpu, "time_to_solution": tts}
     print(json.dumps(line))
     return 0

@@ -52,10 +52,11 @@ typedef struct pf_system pf_system;
  * mixed_switch_ferr > 0 and the handle runs PF_FP32, scft switches to PF_FP64 once
  * ferr < mixed_switch_ferr, or once the FP32 iterations have not lowered ferr by 1% for 200
  * steps (their rounding floor lies above mixed_switch_ferr), and continues to ftol/stol (FP64
- * polish).  polish selects how: 0 = Newton-Krylov steps (each one float64 residual and a
+ * polish).  polish selects how: 2 = Newton-Krylov steps (each one float64 residual and a
  * restarted GMRES over float32 finite-difference Jacobian products; runs without a
  * DomainUpdater; falls back to the field updater's float64 steps if a Newton step stalls),
- * 1 = float64 steps of the field updater (the Anderson history restarted at the switch). */
+ * 1 = float64 steps of the field updater (the Anderson history restarted at the switch),
+ * 0 = automatic: Newton-Krylov on 3D grids, field-updater steps on 1D and 2D grids. */
 typedef struct pf_scft_options {
   int nsteps;
   int nsout;
@@ -257,6 +258,13 @@ int pf_propagate_noalloc_status(void* stream);
  * wait give up at once, which exercises that path in tests without a fault; copies already in
  * flight are still drained with the default limit before a pencil pass exits. */
 int pf_set_wait_limit(pf_system* sys, double seconds);
+
+/* Schedule of the 3D pencil pass for this handle's grid in its current precision: pipeline
+ * stages (2 or 3 tile buffers per CTA) and rounds (tiles per CTA).  The engine's autotuner
+ * picks them by timing real contour steps of each candidate the first time a handle of this
+ * process solves a density on that grid (*tuned = 1 from then on; PF_NO_AUTOTUNE=1 in the
+ * environment keeps the default 3 stages x 2 rounds).  No counterpart in the reference. */
+int pf_get_pencil_schedule(pf_system* sys, int* stages, int* rounds, int* tuned);
 
 /* ---- measurement ---- */
 /* Device time (ms) of the last density solve's propagator launches, measured with CUDA

@@ -541,6 +541,8 @@ struct System {
     if (ng_env && ng_env[0] == '1') use_graphs = false;
     const char* nb_env = getenv("PF_NO_BRANCHES");
     if (nb_env && nb_env[0] == '1') use_branches = false;
+    const char* na_env = getenv("PF_NO_AUTOTUNE");
+    if (na_env && na_env[0] == '1') autotune = false;
   }
   ~System() {
     if (st) cudaStreamSynchronize(st);
@@ -548,6 +550,8 @@ struct System {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     for (auto& e : uev)
+      if (e) cudaEventDestroy(e);
+    for (auto& e : tev)
       if (e) cudaEventDestroy(e);
     for (int b = 0; b < kMaxBranches; ++b) {
       if (br.s[b]) cudaStreamDestroy(br.s[b]);
@@ -1040,8 +1044,10 @@ struct System {
       PF_CU(cudaGraphLaunch(gexec[p], st));
       count_launches(graph_kernels[p]);
     } else if (!graph_warm[p]) {
-      // first solve runs directly (it also sets the kernels' shared-memory attributes)
+      // first solve runs directly (it also sets the kernels' shared-memory attributes); the
+      // pencil-pass schedule is tuned after it, before any capture
       density_enqueue<T>(p);
+      autotune_pencil<T>(p);
       graph_warm[p] = true;
     } else {
       const long l0 = launch_total();
@@ -1076,6 +1082,49 @@ struct System {
       t_dens_ms = b;
     }
     last_prec = p;
+  }
+  // Pencil-pass autotuner.  The first time a 3D handle has solved a density for a transform
+  // length and plane size that no handle of this process has tuned, each candidate schedule
+  // (pipeline stages x tiles per CTA) reruns the first kTuneSteps contour steps of the first
+  // chain (plane and pencil passes, as in a density solve; the rerun rewrites the same values),
+  // once untimed and once timed with CUDA events; the fastest is kept for every later launch.
+  // Schedules differ only in how tiles are distributed, not in arithmetic, so results do not
+  // depend on the choice.  PF_NO_AUTOTUNE=1 keeps the default schedule.
+  bool autotune = true;
+  cudaEvent_t tev[2] = {nullptr, nullptr};
+  template <typename T>
+  void autotune_pencil(int p) {
+    if (nz == 1 || njobs == 0 || mde != 0 || !autotune || capturing) return;
+    const int nkp = (nx / 2 + 1) * ny;
+    if (get_pencil_schedule<T>(nz, nkp, nullptr, nullptr)) return;
+    static const int cands[][2] = {{2, 1}, {2, 2}, {3, 1}, {3, 2}, {3, 4}};
+    constexpr int kTuneSteps = 8;
+    ChainHost<T> h = hosts_of<T>()[0];
+    h.nsteps = std::min(kTuneSteps, h.nsteps);
+    for (auto& e : tev)
+      if (!e) PF_CU(cudaEventCreate(&e));
+    float best = 1e30f;
+    int bs = 0, br = 0;
+    for (const auto& c : cands) {
+      h.zstages = c[0];
+      h.zrounds = c[1];
+      float ms = 0.0f;
+      for (int rep = 0; rep < 2; ++rep) {
+        PF_CU(cudaEventRecord(tev[0], st));
+        launch_chains<T>(jobs[p].as<ChainJob<T>>(), 1, h.nsteps, GridDims{nx, ny, nz}, tw<T>(p), st, &h);
+        PF_CU(cudaEventRecord(tev[1], st));
+        check_launch();
+        PF_CU(cudaEventSynchronize(tev[1]));
+        PF_CU(cudaEventElapsedTime(&ms, tev[0], tev[1]));
+      }
+      if (ms < best) {
+        best = ms;
+        bs = c[0];
+        br = c[1];
+      }
+    }
+    check_pipe(p);
+    set_pencil_schedule<T>(nz, nkp, bs, br);
   }
   void invalidate_graphs() {
     for (int p = 0; p < 2; ++p) {
@@ -2110,7 +2159,11 @@ struct System {
           prec = 0;
           r.switch_step = step;
           if (active == 0) anderson_restart();
-          if (o.polish == 0 && !vcell) {
+          // polish 0 (automatic): Newton-Krylov on 3D grids, where a float64 density solve costs
+          // ~20 float32 ones; on 1D/2D grids a solve is short enough that the field updater's own
+          // float64 steps finish sooner than GMRES cycles with their host round trips
+          const bool newton = o.polish == 2 || (o.polish == 0 && nz > 1);
+          if (newton && !vcell) {
             // float64 polish by Newton-Krylov steps with float32 Jacobian products
             step += 1;
             converged = nk_polish(o, step, ferr, fhelm);
@@ -2649,6 +2702,15 @@ int pf_set_wait_limit(pf_system* sys, double seconds) {
     for (auto& h : s.hosts_f) h.wait_ns = s.wait_ns;
     for (auto& h : s.hosts_d) h.wait_ns = s.wait_ns;
     s.invalidate_graphs();  // captured launches hold the old limit
+  });
+}
+
+int pf_get_pencil_schedule(pf_system* sys, int* stages, int* rounds, int* tuned) {
+  return guard(sys, [&](pf::System& s) {
+    const int nkp = (s.nx / 2 + 1) * s.ny;
+    const bool t = s.prec == 0 ? pf::get_pencil_schedule<double>(s.nz, nkp, stages, rounds)
+                               : pf::get_pencil_schedule<float>(s.nz, nkp, stages, rounds);
+    if (tuned) *tuned = t ? 1 : 0;
   });
 }
 

@@ -118,7 +118,13 @@ struct ChainHost {
   // Time limit (ns of GPU time) of the pencil pass's waits for its tiles; 0 makes them give up
   // at once (failure tests).  The drain of copies in flight keeps the default limit.
   unsigned long long wait_ns = 1000000000ull;
+  // Pencil-pass schedule forced for this chain (stages 2 or 3, rounds = tiles per CTA); 0: the
+  // autotuned schedule of the transform length, else the default.
+  int zstages = 0, zrounds = 0;
 };
+// Autotuned pencil-pass schedules per (precision T, Nz, half-spectrum plane size Nkp).
+template <typename T> void set_pencil_schedule(int nz, int nkp, int stages, int rounds);
+template <typename T> bool get_pencil_schedule(int nz, int nkp, int* stages, int* rounds);
 // 3D grids need hosts (njobs entries); 1D/2D grids ignore it.
 template <typename T>
 void launch_chains(const ChainJob<T>* jobs_dev, int njobs, int maxsteps, const GridDims& d, const Twiddles<T>& tw,

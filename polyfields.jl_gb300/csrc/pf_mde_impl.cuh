@@ -31,6 +31,8 @@
 #include "pf_kernels.h"
 #include "pf_tma.cuh"
 #include <cudaTypedefs.h>
+#include <map>
+#include <mutex>
 #include <stdexcept>
 #include <utility>
 
@@ -626,7 +628,7 @@ __global__ void __launch_bounds__(PlaneCfg<NX, NY>::THREADS, sizeof(T) == 8 ? 1 
 // When a bounded wait gives up, the launch writes 1 to its owner's status word (a per-handle
 // device int, read and cleared by the host) and its output is invalid.
 
-template <typename T, int NZ>
+template <typename T, int NZ, int STAGES_ = 3>
 struct ZPipe {
   static constexpr int E = (int)sizeof(Cx<T>);
   static constexpr int M = 128 / E;              // pencils per tile
@@ -636,10 +638,7 @@ struct ZPipe {
   static constexpr int THREADS = TPC * TT;
   static constexpr int KB = NZ * 128;            // bytes of a spectrum tile
   static constexpr int LB = NZ * M * (int)sizeof(T);  // bytes of an LD tile
-#ifndef PF_ZSTAGES
-#define PF_ZSTAGES 3
-#endif
-  static constexpr int STAGES = PF_ZSTAGES;
+  static constexpr int STAGES = STAGES_;
   static constexpr int SMEM = STAGES * TPC * (KB + LB) + 1024;  // + alignment of the buffers
   // CTAs per SM that the shared memory allows (at most PF_ZMINB): the register budget follows
 #ifndef PF_ZMINB
@@ -733,12 +732,12 @@ __device__ __forceinline__ void ztile_inverse(Cx<T>* kt, int g, const Cx<T>* twa
 // half-spectrum scratch as rows of Nkp elements (8-byte units), lmap the step's LD.  A wait
 // for a tile that gives up after wait_ns sets *status (when not null); the copies already
 // issued are then drained with the default limit before the CTA exits.
-template <typename T, int NZ>
-__global__ void __launch_bounds__(ZPipe<T, NZ>::THREADS, ZPipe<T, NZ>::MINB)
+template <typename T, int NZ, int STAGES>
+__global__ void __launch_bounds__(ZPipe<T, NZ, STAGES>::THREADS, ZPipe<T, NZ, STAGES>::MINB)
     z_pipe_kernel(const __grid_constant__ CUtensorMap kmap, const __grid_constant__ CUtensorMap lmap,
                   float* __restrict__ csc, double* __restrict__ lsc, int t, int ntiles, double ng, Twiddles<T> twg,
                   int* __restrict__ status, unsigned long long wait_ns) {
-  using Z = ZPipe<T, NZ>;
+  using Z = ZPipe<T, NZ, STAGES>;
   constexpr int S = Z::STAGES, TPC = Z::TPC, G = Z::G;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sbase = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -1217,20 +1216,32 @@ static void launch_on(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sm
   if (e != cudaSuccess) throw DeviceError(std::string("kernel launch failed: ") + cudaGetErrorString(e));
 }
 
-// rounds (stages of tiles) per CTA of the pencil pipeline
-#ifndef PF_ZRPC
-#define PF_ZRPC 2
-#endif
-constexpr int kZRoundsPerCta = PF_ZRPC;
+// Pencil-pass schedules: pipeline stages (2 or 3 tile buffers per CTA) and rounds (tiles per
+// CTA, which sets the grid).  The choice per (precision, Nz, plane size) comes from the
+// autotuner (System::autotune_pencil: real chain steps timed per candidate when a handle first
+// builds its 3D chains) or, before tuning, the default below; a chain may also force one.
+constexpr int kZDefaultStages = 3, kZDefaultRounds = 2;
+struct ZSchedule {
+  int stages = kZDefaultStages, rounds = kZDefaultRounds;
+};
+template <typename T>
+struct ZScheduleTable {
+  std::mutex mu;
+  std::map<std::pair<int, int>, ZSchedule> tuned;  // (Nz, Nkp) -> schedule
+  static ZScheduleTable& get() {
+    static ZScheduleTable t;
+    return t;
+  }
+};
 
-template <typename T, int NZ>
-static void launch_z_pipe(const ChainHost<T>& h, int t, int nkp, double ng, const Twiddles<T>& tw,
-                          cudaStream_t st) {
-  using Z = ZPipe<T, NZ>;
+template <typename T, int NZ, int S>
+static void launch_z_pipe_s(const ChainHost<T>& h, int t, int nkp, double ng, const Twiddles<T>& tw, int rounds,
+                            cudaStream_t st) {
+  using Z = ZPipe<T, NZ, S>;
   static const int grid_cap = [] {  // thread-safe one-time setup
-    set_smem(z_pipe_kernel<T, NZ>, Z::SMEM);
+    set_smem(z_pipe_kernel<T, NZ, S>, Z::SMEM);
     int occ = 0, dev = 0, nsm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, z_pipe_kernel<T, NZ>, Z::THREADS, Z::SMEM);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, z_pipe_kernel<T, NZ, S>, Z::THREADS, Z::SMEM);
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     return (occ > 0 ? occ : 1) * (nsm > 0 ? nsm : 1);
@@ -1239,12 +1250,29 @@ static void launch_z_pipe(const ChainHost<T>& h, int t, int nkp, double ng, cons
   make_zmaps<T>(&km, &lm, h.kbuf, h.ld[t], nkp, NZ);
   const int ntiles = (nkp + Z::M - 1) / Z::M;
   const int nrounds = (ntiles + Z::TPC - 1) / Z::TPC;
-  int grid = (nrounds + kZRoundsPerCta - 1) / kZRoundsPerCta;
+  int grid = (nrounds + rounds - 1) / rounds;
   if (grid > grid_cap) grid = grid_cap;
   if (grid < 1) grid = 1;
-  launch_on(z_pipe_kernel<T, NZ>, dim3(grid), dim3(Z::THREADS), Z::SMEM, st, true, km, lm, h.csc, h.lsc, t,
+  launch_on(z_pipe_kernel<T, NZ, S>, dim3(grid), dim3(Z::THREADS), Z::SMEM, st, true, km, lm, h.csc, h.lsc, t,
             ntiles, ng, tw, h.status, h.wait_ns);
   count_launches(1);
+}
+
+template <typename T, int NZ>
+static void launch_z_pipe(const ChainHost<T>& h, int t, int nkp, double ng, const Twiddles<T>& tw,
+                          cudaStream_t st) {
+  ZSchedule z;
+  if (h.zstages > 0) {
+    z.stages = h.zstages;
+    z.rounds = h.zrounds > 0 ? h.zrounds : kZDefaultRounds;
+  } else {
+    auto& tab = ZScheduleTable<T>::get();
+    std::lock_guard<std::mutex> lock(tab.mu);
+    auto it = tab.tuned.find({NZ, nkp});
+    if (it != tab.tuned.end()) z = it->second;
+  }
+  if (z.stages == 2) launch_z_pipe_s<T, NZ, 2>(h, t, nkp, ng, tw, z.rounds, st);
+  else launch_z_pipe_s<T, NZ, 3>(h, t, nkp, ng, tw, z.rounds, st);
 }
 
 template <typename T>
@@ -1260,6 +1288,23 @@ static void z_pipe_dispatch(int nz, const ChainHost<T>& h, int t, int nkp, doubl
     default:
       return;
   }
+}
+
+template <typename T>
+void set_pencil_schedule(int nz, int nkp, int stages, int rounds) {
+  auto& tab = ZScheduleTable<T>::get();
+  std::lock_guard<std::mutex> lock(tab.mu);
+  tab.tuned[{nz, nkp}] = ZSchedule{stages, rounds};
+}
+template <typename T>
+bool get_pencil_schedule(int nz, int nkp, int* stages, int* rounds) {
+  auto& tab = ZScheduleTable<T>::get();
+  std::lock_guard<std::mutex> lock(tab.mu);
+  auto it = tab.tuned.find({nz, nkp});
+  const ZSchedule z = it != tab.tuned.end() ? it->second : ZSchedule{};
+  if (stages) *stages = z.stages;
+  if (rounds) *rounds = z.rounds;
+  return it != tab.tuned.end();
 }
 
 template <typename T, int NX, int NY>
@@ -1481,6 +1526,8 @@ void launch_stress(const StressItem<T>* items, int nitems, const T* const* src_q
 #define PF_INST(T)                                                                                         \
   template bool shape_supported<T>(int, int, int);                                                         \
   template void launch_lw<T>(T*, const double*, double, long, cudaStream_t);                              \
+  template void set_pencil_schedule<T>(int, int, int, int);                                                \
+  template bool get_pencil_schedule<T>(int, int, int*, int*);                                              \
   template void launch_ld<T>(T*, const CellGeom&, double, double, long, cudaStream_t);                    \
   template void launch_fill<T>(T*, T, long, cudaStream_t);                                                \
   template void launch_chains<T>(const ChainJob<T>*, int, int, const GridDims&, const Twiddles<T>&,       \

@@ -27,7 +27,7 @@ struct PFOptions            # pf_scft_options
     nsteps::Cint
     nsout::Cint
     nsave::Cint
-    polish::Cint              # 0 Newton-Krylov polish, 1 float64 field-updater steps
+    polish::Cint              # 0 automatic, 1 float64 field-updater steps, 2 Newton-Krylov polish
     ftol::Cdouble
     stol::Cdouble
     mixed_switch_ferr::Cdouble

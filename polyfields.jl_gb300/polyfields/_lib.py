@@ -87,6 +87,7 @@ SIGNATURES = {
     "pf_propagate_noalloc": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _c_int, _vp]),
     "pf_propagate_noalloc_status": (_c_int, [_vp]),
     "pf_set_wait_limit": (_c_int, [_vp, _c_double]),
+    "pf_get_pencil_schedule": (_c_int, [_vp, _iptr, _iptr, _iptr]),
     "pf_set_timing": (_c_int, [_vp, _c_int]),
     "pf_last_timing": (_c_int, [_vp, _dptr, _dptr, _iptr]),
     "pf_record_event": (_c_int, [_vp, _c_int]),

@@ -460,6 +460,14 @@ class FieldSystem:
         such wait give up at once (exercises the timeout path in tests)."""
         L.check(L.load().pf_set_wait_limit(self._h, float(seconds)), self._h)
 
+    def pencil_schedule(self):
+        """(stages, rounds, tuned) of the 3D pencil pass for this grid and precision: the
+        autotuner's choice once a density has been solved on this grid (tuned True)."""
+        a, b, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        L.check(L.load().pf_get_pencil_schedule(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(t)),
+                self._h)
+        return a.value, b.value, bool(t.value)
+
     def set_timing(self, enable: bool) -> None:
         L.check(L.load().pf_set_timing(self._h, 1 if enable else 0), self._h)
 
@@ -667,8 +675,8 @@ class SCFTOptions:
     then continue in fp64 (0 disables the switch).  ``polish`` selects the fp64 phase:
     "newton" (Newton-Krylov steps: one fp64 residual each, the linear solve by GMRES over
     fp32 finite-difference Jacobian products; runs without a DomainUpdater, falls back to the
-    updater's fp64 steps if a Newton step stalls) or "updater" (fp64 steps of the field
-    updater)."""
+    updater's fp64 steps if a Newton step stalls), "updater" (fp64 steps of the field
+    updater), or "auto" (Newton-Krylov on 3D grids, updater steps on 1D/2D grids)."""
     nsteps: int = 100
     nsout: int = 0
     nsave: int = 0
@@ -676,7 +684,7 @@ class SCFTOptions:
     stol: float = 1e-4
     savepath: str = ""
     mixed_switch_ferr: float = 0.0
-    polish: str = "newton"
+    polish: str = "auto"
 
 
 @dataclass
@@ -693,7 +701,7 @@ class SCFTResults:
     polish_fp32_solves: int = 0
 
 
-_POLISH = {"newton": 0, "updater": 1}
+_POLISH = {"auto": 0, "updater": 1, "newton": 2}
 
 
 def _options(opts: "SCFTOptions"):

@@ -384,3 +384,19 @@ def test_grand_ensemble(prec, tol):
         assert rel(g.residuals[mid], o.residuals[mid]) < 10 * tol, mid
     assert g.free_energy() == pytest.approx(o.free_energy(), rel=tol)
     assert np.allclose(g.scfstress(), o.scfstress(), rtol=1e-9 if prec == "fp64" else 2e-3, atol=1e-12)
+
+
+def test_pencil_schedule_is_autotuned_on_first_solve():
+    """The first density solve on a 3D grid tunes the pencil pass's schedule (stages x tiles
+    per CTA) by timing real contour steps; later solves use it and still match the oracle."""
+    kw = dict(dims=(32, 32, 32), crystal="cubic", params=(7.0,), f=0.3, Ns=60, amp=0.15)
+    g = SY.diblock_system(pf, precision="fp32", **kw)
+    stages, rounds, tuned = g.pencil_schedule()
+    assert tuned and stages in (2, 3) and rounds in (1, 2, 4)
+    o = SY.diblock_system(O, **kw)
+    o.density_update()
+    for _ in range(3):  # replayed graphs use the tuned schedule
+        g.density_update()
+    assert g.species[0].Q == pytest.approx(o.species[0].Q, rel=FP32_RTOL)
+    for mid in (1, 2):
+        assert rel(g.density[mid], o.density[mid]) < FP32_RTOL

@@ -7,6 +7,9 @@ N_A 31, a0 7.42): every cell update moves the cell by the step cap until the pro
 overflow and scft! stops with "Diverging field updater -- breaking." (src/simulate.jl:109-111).
 The GPU engine does the same (tests/test_gpu_vcell.py); it is the algorithm's behaviour on
 this system, not an effect of precision.
+
+The reference's stress also depends on where the structure sits in the box, so the converged
+cell does too (second test).
 """
 import numpy as np
 import pytest
@@ -34,3 +37,53 @@ def test_oracle_domain_updater_runs_away_and_diverges():
     # the first two updates each move a0 by about nper * rlxn * lam * pmax = 0.95
     assert cells[0] == pytest.approx(INSTANCE["a0"] + 0.95, abs=1e-6)
     assert cells[1] == pytest.approx(INSTANCE["a0"] + 1.90, abs=1e-6)
+
+
+def _lamellar(L, scale, amp, seed=1):
+    return W.diblock_system(O, dims=(64, 1, 1), crystal="lamellar", params=(L,), scale=scale, amp=amp, seed=seed)
+
+
+def _scft_vcell(s):
+    return O.scft(s, O.AndersonUpdater(nhist=10), domain=O.DomainUpdater(nskip=5, nper=20),
+                  opts=O.SCFTOptions(nsteps=3000, ftol=1e-9, stol=1e-9))
+
+
+def _settle(s):
+    """scft! again until a call converges at entry, where the stress is computed afresh."""
+    r = _scft_vcell(s)
+    for _ in range(6):
+        assert r.converged
+        if r.nsteps == 0:
+            return r
+        r = _scft_vcell(s)
+    raise AssertionError("no call converged at entry")
+
+
+def _phase(s):
+    """Position of the lamella: phase of the first Fourier mode of w_A, in periods."""
+    return float(np.angle(np.fft.rfft(s.fields[1].ravel())[1]) / (2 * np.pi))
+
+
+def test_oracle_converged_cell_depends_on_the_structure_position():
+    """The reference's stress is sum_k Re(q_k) Re(qc_k) dksq_k (multiblock.jl:279-282): it
+    changes when the structure is translated, which the field iteration leaves free.  Float64
+    runs of the README lamellar system from two noisy starts (L0 = 13, seeds 1 and 3) end with
+    ferr and a freshly computed stress below 1e-9 (scft! is called again until a call converges
+    at entry) with the lamella 0.002 and 0.021 periods off the origin, in cells 2e-3 apart and
+    with different free energies.  From a mirror-symmetric cosine start (real spectra) the
+    lamella stays at the origin and the cell is 16.51651."""
+    cells, fhelms, phases = [], [], []
+    for seed in (1, 3):
+        s = _lamellar(13.0, scale=0.1, amp=0.5, seed=seed)
+        r = _settle(s)
+        cells.append(float(s.cell.params[0]))
+        fhelms.append(r.fhelm)
+        phases.append(abs(_phase(s)))
+    assert phases[0] == pytest.approx(0.0019, abs=2e-4) and phases[1] == pytest.approx(0.0206, abs=2e-4)
+    assert abs(cells[0] - cells[1]) > 1e-3 * cells[0]
+    assert abs(fhelms[0] - fhelms[1]) > 1e-6
+    sym = _lamellar(13.0, scale=0.0, amp=0.5)
+    _settle(sym)
+    assert abs(_phase(sym)) < 1e-5
+    assert float(sym.cell.params[0]) == pytest.approx(16.51651036, rel=1e-8)
+    assert cells[0] < float(sym.cell.params[0])
