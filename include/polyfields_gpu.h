@@ -216,9 +216,13 @@ int pf_free_energy_pullback(pf_system* sys, double* cell_bar, int ncell, double*
  * FieldSystem) driven together: nthreads host threads (0: min(n, 32)) take the systems in
  * decreasing order of cost (grid points x contour steps) and run pf_scft on each, every
  * system on its own CUDA stream (density solves launched directly, not replayed as CUDA
- * graphs), so the GPU runs up to nthreads solves at once.  results[i] and status[i] receive system i's outcome
- * (pf_last_error(systems[i]) its message); returns PF_OK when every run returned PF_OK, else
- * the first nonzero status in index order.  A handle must not be used elsewhere meanwhile. */
+ * graphs), so the GPU runs up to nthreads solves at once.  results[i] and status[i] receive
+ * system i's outcome (pf_last_error(systems[i]) its message); returns PF_OK when every run
+ * returned PF_OK, else the first nonzero status in index order.  A handle must not be used
+ * elsewhere meanwhile.  Streams beyond the runtime's hardware work queues share queues and wait
+ * on one another: the library sets CUDA_DEVICE_MAX_CONNECTIONS=32 when it is loaded (unless the
+ * variable is already set), which only takes effect if the process creates its CUDA context
+ * afterwards; a caller that initialises CUDA first should set it itself. */
 int pf_scft_batch(pf_system* const* systems, int n, const pf_scft_options* opts, int use_domain,
                   pf_scft_results* results, int* status, int nthreads);
 

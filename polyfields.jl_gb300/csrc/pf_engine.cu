@@ -395,6 +395,15 @@ static void chain_grid(const std::vector<double>& Nb, int Ns, double& N, std::ve
 }
 
 // ------------------------------------------------------------------ the system
+// Handles run on their own streams, batched ones from their own host threads (pf_scft_batch).
+// The CUDA runtime maps the streams of a process onto CUDA_DEVICE_MAX_CONNECTIONS hardware work
+// queues (8 unless set), and streams that share a queue wait on one another's work.  When the
+// library is loaded it asks for the maximum, 32, unless the caller has set the variable; this
+// takes effect only if the process has not created its CUDA context yet.
+__attribute__((constructor)) static void pf_request_connections() {
+  setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
+}
+
 struct System {
   int nx, ny, nz;
   long ng, nk;
@@ -462,6 +471,33 @@ struct System {
   cudaEvent_t uev[8] = {};  // user events (pf_record_event)
   double t_prop_ms = 0.0, t_dens_ms = 0.0;
   int mde_steps = 0;
+  // Small device-to-host reads (status words, Q, reduction results) land in this handle's pinned
+  // staging buffer.  A read into pageable memory is staged by the driver through buffers shared
+  // by the whole process, and with many handles stepping on their own threads (pf_scft_batch)
+  // those reads queued behind one another: 32 identical 2D systems on 32 threads advanced about
+  // three at a time.  With this buffer and 32 hardware queues (pf_request_connections) they run
+  // side by side.
+  static constexpr size_t kPinBytes = 64 * 1024;
+  unsigned char* hpin = nullptr;
+  // Queue a read of `bytes` from device address src into the staging buffer at byte offset off;
+  // the data is valid after the next sync_st().
+  void d2h_pin(size_t off, const void* src, size_t bytes) {
+    if (off + bytes > kPinBytes) throw PFError(E_ARG, "pinned staging buffer too small");
+    PF_CU(cudaMemcpyAsync(hpin + off, src, bytes, cudaMemcpyDeviceToHost, st));
+  }
+  // Read `bytes` from device address src into dst and wait for it.
+  void d2h_now(void* dst, const void* src, size_t bytes) {
+    if (bytes <= kPinBytes) {
+      d2h_pin(0, src, bytes);
+      sync_st();
+      std::memcpy(dst, hpin, bytes);
+    } else {
+      PF_CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+      sync_st();
+    }
+  }
+  // Host wait on the handle's stream.
+  void sync_st() { PF_CU(cudaStreamSynchronize(st)); }
 
   // Anderson updater (src/updaters/anderson.jl:13-47)
   struct Anderson {
@@ -520,6 +556,7 @@ struct System {
     ng = (long)nx * ny * nz;
     nk = (long)(nx / 2 + 1) * ny * nz;
     PF_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    PF_CU(cudaHostAlloc(reinterpret_cast<void**>(&hpin), kPinBytes, cudaHostAllocDefault));
     part.alloc(sizeof(double) * (size_t)kRedBlocks * 4 * (kMaxMon + 1) + sizeof(double) * 2048 * 2 * 152);
     sums.alloc(sizeof(double) * 4 * kMaxMon);
     stats4.alloc(sizeof(double) * 8);
@@ -553,6 +590,7 @@ struct System {
       if (e) cudaEventDestroy(e);
     for (auto& e : tev)
       if (e) cudaEventDestroy(e);
+    if (hpin) cudaFreeHost(hpin);
     for (int b = 0; b < kMaxBranches; ++b) {
       if (br.s[b]) cudaStreamDestroy(br.s[b]);
       if (br.join[b]) cudaEventDestroy(br.join[b]);
@@ -653,7 +691,7 @@ struct System {
                                 cudaMemcpyDeviceToDevice, st));
         }
       }
-      PF_CU(cudaStreamSynchronize(st));
+      sync_st();
       std::swap(b->p, nb.p);
       std::swap(b->bytes, nb.bytes);
     }
@@ -1150,22 +1188,28 @@ struct System {
   void check_pipe(int = 0) {
     int v = 0;
     if (nz > 1) {  // 1D/2D chains have no pencil pass
-      PF_CU(cudaMemcpyAsync(&v, pipe_st.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+      d2h_pin(kPinBytes - sizeof(int), pipe_st.p, sizeof(int));
       PF_CU(cudaMemsetAsync(pipe_st.p, 0, sizeof(int), st));
     }
-    PF_CU(cudaStreamSynchronize(st));
+    sync_st();
+    if (nz > 1) std::memcpy(&v, hpin + kPinBytes - sizeof(int), sizeof(int));
     if (v)
       throw PFError(E_TIMEOUT, "pencil pass: a TMA copy did not complete within its time limit; the last density "
                                "solve is invalid");
   }
   void fetch_Q() {
+    size_t k = 0;
     for (auto& sp : species) {
-      if (!sp->Q_valid) {
-        PF_CU(cudaMemcpyAsync(&sp->Q, sp->Qdev.p, sizeof(double), cudaMemcpyDeviceToHost, st));
-      }
+      if (!sp->Q_valid) d2h_pin(sizeof(double) * k, sp->Qdev.p, sizeof(double));
+      ++k;
     }
-    PF_CU(cudaStreamSynchronize(st));
+    sync_st();
     check_pipe(last_prec);
+    k = 0;
+    for (auto& sp : species) {
+      if (!sp->Q_valid) std::memcpy(&sp->Q, hpin + sizeof(double) * k, sizeof(double));
+      ++k;
+    }
     for (auto& sp : species) {
       sp->Q_valid = true;
       if (ensemble == 0) {
@@ -1192,8 +1236,9 @@ struct System {
                  stats4.as<double>(), st);
     check_launch();
     double s[4];
-    PF_CU(cudaMemcpyAsync(s, stats4.p, sizeof(s), cudaMemcpyDeviceToHost, st));
+    d2h_pin(0, stats4.p, sizeof(s));
     check_pipe();  // also synchronises: a timed-out pencil pass invalidates these sums
+    std::memcpy(s, hpin, sizeof(s));
     ferr = std::sqrt(s[0]) / std::sqrt(2.220446049250313e-16 + s[1]);
     double ftrans = 0.0;
     for (auto& sp : species) {
@@ -1232,8 +1277,7 @@ struct System {
                  stats4.as<double>(), st);
     check_launch();
     double s[4];
-    PF_CU(cudaMemcpyAsync(s, stats4.p, sizeof(s), cudaMemcpyDeviceToHost, st));
-    PF_CU(cudaStreamSynchronize(st));
+    d2h_now(s, stats4.p, sizeof(s));
     if (s[1] == 0.0) throw PFError(E_ARG, "Fields must be initialized before SCFT simulation.");
     double phisum = 0.0;
     for (auto& sp : species) phisum += sp->phi;
@@ -1280,8 +1324,7 @@ struct System {
     std::vector<int> item_s;
     if (scaled(p)) {
       hfac.resize(sp.Ns + 1);
-      PF_CU(cudaMemcpyAsync(hfac.data(), sp.fac.p, sizeof(double) * (sp.Ns + 1), cudaMemcpyDeviceToHost, st));
-      PF_CU(cudaStreamSynchronize(st));
+      d2h_now(hfac.data(), sp.fac.p, sizeof(double) * (sp.Ns + 1));
       for (int b = 0; b < sp.nblocks(); ++b)
         for (int s = sp.begin_block[b]; s <= sp.begin_block[b + 1]; ++s) item_s.push_back(s - 1);
     }
@@ -1296,8 +1339,7 @@ struct System {
       launch_stress<T>(di.as<StressItem<T>>(), nit, nullptr, nullptr, nullptr, nullptr, d, dksq.as<double>(), npr,
                        dp.as<double>(), tw<T>(p), st);
       check_launch();
-      PF_CU(cudaMemcpyAsync(qint.data(), dp.p, dp.bytes, cudaMemcpyDeviceToHost, st));
-      PF_CU(cudaStreamSynchronize(st));
+      d2h_now(qint.data(), dp.p, dp.bytes);
     } else {
       const int M = zM(p);
       const int nkp = (nx / 2 + 1) * ny;
@@ -1324,8 +1366,7 @@ struct System {
                          (Cx<T>* const*)(pp + 2 * chunk), (Cx<T>* const*)(pp + 3 * chunk), d, dksq.as<double>(), npr,
                          dp.as<double>(), tw<T>(p), st);
         check_launch();
-        PF_CU(cudaMemcpyAsync(hp.data(), dp.p, sizeof(double) * (size_t)cn_ * ntiles * npr, cudaMemcpyDeviceToHost, st));
-        PF_CU(cudaStreamSynchronize(st));
+        d2h_now(hp.data(), dp.p, sizeof(double) * (size_t)cn_ * ntiles * npr);
         for (int i = 0; i < cn_; ++i)
           for (int k = 0; k < npr; ++k) {
             double s = 0.0;
@@ -1476,8 +1517,7 @@ struct System {
     double* hd = nkb.h.as<double>() + 3 * (kNKRestart + 2);
     launch_multidot(a, 1, n, b, nkb.part.as<double>(), hd, st);
     double v = 0.0;
-    PF_CU(cudaMemcpyAsync(&v, hd, sizeof(double), cudaMemcpyDeviceToHost, st));
-    PF_CU(cudaStreamSynchronize(st));
+    d2h_now(&v, hd, sizeof(double));
     return v;
   }
   // z = (F32(wk + e v) - F32(wk)) / e with e = kNKStep |wk| / vnorm
@@ -1548,8 +1588,7 @@ struct System {
           launch_multiaxpy(z, V, j + 1, n, hd + (m + 1), 1.0, -1.0, st);
           launch_multidot(z, 1, n, z, nkb.part.as<double>(), hd + 2 * (m + 1), st);
           check_launch();
-          PF_CU(cudaMemcpyAsync(hh.data(), hd, sizeof(double) * (2 * (m + 1) + 1), cudaMemcpyDeviceToHost, st));
-          PF_CU(cudaStreamSynchronize(st));
+          d2h_now(hh.data(), hd, sizeof(double) * (2 * (m + 1) + 1));
           for (int i = 0; i <= j; ++i) H[(size_t)i * m + j] = hh[i] + hh[m + 1 + i];
           const double hn = std::sqrt(std::max(0.0, hh[2 * (m + 1)]));
           H[(size_t)(j + 1) * m + j] = hn;
@@ -1654,15 +1693,13 @@ struct System {
       launch_solve(packed.as<double>(), ih, cn.as<double>(), status.as<int>(), st);
       check_launch();
       int sv[2] = {0, 0};
-      PF_CU(cudaMemcpyAsync(sv, status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
-      PF_CU(cudaStreamSynchronize(st));
+      d2h_now(sv, status.p, sizeof(int) * 2);
       if (sv[1] != 0) {
         // cancellation guard of the expanded sums: sum U and V directly
         launch_gram(h, ih, nall, part.as<double>(), packed.as<double>(), st);
         launch_solve(packed.as<double>(), ih, cn.as<double>(), status.as<int>(), st);
         check_launch();
-        PF_CU(cudaMemcpyAsync(sv, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-        PF_CU(cudaStreamSynchronize(st));
+        d2h_now(sv, status.p, sizeof(int));
       }
       if (sv[0] != 0)
         throw PFError(E_SINGULAR, "Error inverting Umn matrix on iteration " + std::to_string(it) +
@@ -1815,8 +1852,7 @@ struct System {
     auto dot_host = [&](const double* a, const double* b) {
       launch_ddot(a, b, ng, dpart.as<double>(), dots.as<double>(), st);
       double v = 0.0;
-      PF_CU(cudaMemcpyAsync(&v, dots.p, sizeof(double), cudaMemcpyDeviceToHost, st));
-      PF_CU(cudaStreamSynchronize(st));
+      d2h_now(&v, dots.p, sizeof(double));
       return v;
     };
     for (auto& spp : species) {
@@ -1855,8 +1891,7 @@ struct System {
       }
       double meanq = sp.Q;
       if (scaled(p)) {
-        PF_CU(cudaMemcpyAsync(&meanq, sp.meanq.p, sizeof(double), cudaMemcpyDeviceToHost, st));
-        PF_CU(cudaStreamSynchronize(st));
+        d2h_now(&meanq, sp.meanq.p, sizeof(double));
       }
       const double dq = -S / (meanq * (double)ng);  // through Q = mean(q_Ns), rescaled
       for (int b = 0; b < nb; ++b)
@@ -1991,7 +2026,7 @@ struct System {
       }
       jobidx += homo ? 1 : 2;
     }
-    PF_CU(cudaStreamSynchronize(st));
+    sync_st();
     check_pipe(p);
   }
   void pullback(std::vector<double>& cell_bar, std::vector<double>& nref_bar, bool recompute = true) {
@@ -2024,8 +2059,7 @@ struct System {
     auto dot = [&](const double* a, const double* b) {
       launch_ddot(a, b, ng, dp.as<double>(), dd.as<double>(), st);
       double v = 0.0;
-      PF_CU(cudaMemcpyAsync(&v, dd.p, sizeof(double), cudaMemcpyDeviceToHost, st));
-      PF_CU(cudaStreamSynchronize(st));
+      d2h_now(&v, dd.p, sizeof(double));
       return v;
     };
     chi_bar.clear();
@@ -2047,7 +2081,7 @@ struct System {
       for (int b = 0; b < sp->nblocks() && k < nref_bar.size(); ++b) nref_bar[k++] += t;
     }
     check_launch();
-    PF_CU(cudaStreamSynchronize(st));
+    sync_st();
     return fhelm;
   }
 
@@ -2065,8 +2099,7 @@ struct System {
   // crystal, cell_params, field_type and the fields as nested [z][y][x] lists, one per monomer id.
   void save_fields(const std::string& path) {
     std::vector<double> h((size_t)ng * nmon());
-    PF_CU(cudaMemcpyAsync(h.data(), w.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
-    PF_CU(cudaStreamSynchronize(st));
+    d2h_now(h.data(), w.p, sizeof(double) * h.size());
     FILE* f = fopen(path.c_str(), "w");
     if (!f) throw PFError(E_ARG, "cannot open " + path + " for writing");
     char date[32] = "";
@@ -2231,8 +2264,7 @@ struct System {
     launch_chains<T>(job.as<ChainJob<T>>(), 1, nsteps, GridDims{nx, ny, nz}, tw<T>(p), st, &host);
     check_launch();
     std::vector<T> ho(ng);
-    PF_CU(cudaMemcpyAsync(ho.data(), hist.as<T>() + (long)nsteps * ng, sizeof(T) * ng, cudaMemcpyDeviceToHost, st));
-    PF_CU(cudaStreamSynchronize(st));
+    d2h_now(ho.data(), hist.as<T>() + (long)nsteps * ng, sizeof(T) * ng);
     check_pipe(p);
     for (long i = 0; i < ng; ++i) qout[i] = (double)ho[i];
   }
