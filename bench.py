@@ -290,7 +290,21 @@ def run_gpu(args):
         L.check(lib.pf_elapsed_ms(sysm._h, 2, 3, ctypes.byref(m64)), sysm._h)
         a64, _, _ = sysm.last_timing()
         fp64 = {"iters_per_s": 1000.0 * args.fp64_steps / m64.value, "ms_per_iter": m64.value / args.fp64_steps,
-                "mde_step_us": 1000.0 * a64 / nmde}
+                "mde_step_us": 1000.0 * a64 / nmde, "steps": args.fp64_steps}
+        # the same iteration end to end through the C ABI with host fields (as `e2e` above), the
+        # like-for-like figure against the FP64 CPU restatement
+        for m in (1, 2):
+            L.check(lib.pf_get_grid(sysm._h, L.PF_FIELD, m, L.dptr(host[m])), sysm._h)
+        sysm.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            for m in (1, 2):
+                L.check(lib.pf_set_field(sysm._h, m, L.dptr(host[m])), sysm._h)
+            upd.step()
+            for m in (1, 2):
+                L.check(lib.pf_get_grid(sysm._h, L.PF_FIELD, m, L.dptr(host[m])), sysm._h)
+            _ = sysm.free_energy()
+        fp64["e2e_iters_per_s"] = e2e_steps / (time.perf_counter() - t0)
 
     cpu = cpu_baseline_sample() if args.cpu_seconds > 0 else None
     del upd, sysm
@@ -416,7 +430,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=N_GRID, help="grid points per axis (default 128)")
-    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=1.0, help="CPU baseline sample (0: skip; else one iteration)")
     ap.add_argument("--mode", default="iter", choices=["iter", "tts", "sweep", "profile"])
     ap.add_argument("--seeds", type=int, default=3, help="tts: seeds of the time-to-solution runs")
@@ -426,7 +440,7 @@ def main():
     ap.add_argument("--ns", type=int, default=20, help="profile: contour steps per chain")
     ap.add_argument("--solves", type=int, default=3, help="profile: density solves")
     ap.add_argument("--count", type=int, default=256, help="sweep: instances")
-    ap.add_argument("--nthreads", type=int, default=32, help="sweep: host threads")
+    ap.add_argument("--nthreads", type=int, default=64, help="sweep: host threads")
     ap.add_argument("--sweep-domain", action="store_true", help="sweep: variable cells (DomainUpdater)")
     args = ap.parse_args()
     if args.impl == "reference":

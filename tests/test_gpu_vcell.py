@@ -57,6 +57,35 @@ def test_runaway_cell_tracks_the_oracle_and_diverges():
                 opts=pf.SCFTOptions(nsteps=400, ftol=1e-7, stol=1e-7))
 
 
+def test_bcc_cell_trajectory_tracks_the_oracle():
+    """The BCC workload (AB diblock fA 0.3, chi 0.2, cubic L0 = 7, the 12 {110} cosines plus 0.1
+    noise) at 16^3 with Anderson nhist 10 and DomainUpdater nskip 5 / nper 20, float64: through
+    the first 30 iterations of scft!'s loop (simulate.jl:86-103, six cell updates) the GPU's cell
+    after every update equals the oracle's to 1e-6.  The reference's cell steps back and forth
+    by the step cap (nper rlxn lam pmax = 0.95) and then walks away from 7 (the oracle, run on,
+    leaves it near 15 after 300 iterations without converging): it is the reference iteration,
+    not the GPU, that does not settle this cell."""
+    o = W.bcc_system(O, n=16)
+    g = W.bcc_system(pf, n=16, precision="fp64")
+    uo, ug = O.AndersonUpdater(nhist=10), pf.AndersonUpdater(nhist=10)
+    do, dg = O.DomainUpdater(nskip=5, nper=20), pf.DomainUpdater(nskip=5, nper=20)
+    uo.setup(o)
+    ug.setup(g)
+    do.setup(o)
+    dg.setup(g)
+    cells = []
+    for step in range(30):
+        uo.step()
+        ug.step()
+        if step % 5 == 0:
+            do.step(nsteps=20)
+            dg.step(nsteps=20)
+            cells.append(float(o.cell.params[0]))
+            assert float(g.cell.params[0]) == pytest.approx(cells[-1], rel=1e-6), step
+    assert cells[0] == pytest.approx(7.95, abs=1e-6) and cells[1] == pytest.approx(8.90, abs=1e-6)
+    assert cells[-1] > 10.0
+
+
 def _mixed_vs_fp64(make, updater, domain, ftol, stol, nsteps):
     g64 = make("fp64")
     r64 = pf.scft(g64, updater(), domain=domain(), opts=pf.SCFTOptions(nsteps=nsteps, ftol=ftol, stol=stol))
