@@ -215,8 +215,8 @@ int pf_free_energy_pullback(pf_system* sys, double* cell_bar, int ncell, double*
 /* Many independent scft! runs (a phase-diagram sweep: src/simulate.jl:60-148 once per
  * FieldSystem) driven together: nthreads host threads (0: min(n, 32)) take the systems in
  * decreasing order of cost (grid points x contour steps) and run pf_scft on each, every
- * system on its own CUDA stream (density solves launched directly, not replayed as CUDA
- * graphs), so the GPU runs up to nthreads solves at once.  results[i] and status[i] receive
+ * system on its own CUDA stream (density solves replayed from captured CUDA graphs as in
+ * single runs), so the GPU runs up to nthreads solves at once.  results[i] and status[i] receive
  * system i's outcome (pf_last_error(systems[i]) its message); returns PF_OK when every run
  * returned PF_OK, else the first nonzero status in index order.  A handle must not be used
  * elsewhere meanwhile.  Streams beyond the runtime's hardware work queues share queues and wait

@@ -2693,13 +2693,9 @@ int pf_scft_batch(pf_system* const* systems, int n, const pf_scft_options* opts,
   int dev = 0;
   cudaGetDevice(&dev);
   std::atomic<int> next{0};
-  // Batched systems run their density solves as direct launches.  With many worker threads
-  // each replaying its own small graphs, the 256-instance 2D sweep ran 15% slower (53-54 s
-  // against 46.5 s with direct launches).
-  for (int i = 0; i < n; ++i) {
-    systems[i]->s->use_graphs = false;
-    systems[i]->s->invalidate_graphs();
-  }
+  // Batched systems replay their captured density-solve graphs like single runs.  (Under the
+  // process-wide staging of pageable reads this was 15% slower than direct launches; with
+  // pinned reads and 32 hardware queues the two take the same time.)
   auto worker = [&]() {
     cudaSetDevice(dev);
     for (;;) {
