@@ -404,7 +404,7 @@ def run_sweep(args):
     params = W.hex_sweep_params(args.count, 12345)
     t0 = time.perf_counter()
     res = S.run_sharded(params, rank, world, precision=args.precision, nsteps=3000, nthreads=args.nthreads,
-                        vcell=args.sweep_domain)
+                        vcell=args.sweep_domain, polish=args.polish)
     wall = time.perf_counter() - t0
     if rank == 0:
         iters = sum(r["iterations"] for r in res)
@@ -412,7 +412,7 @@ def run_sweep(args):
             "mode": "sweep", "metric": "instances/s", "value": args.count / wall, "unit": "instances/s",
             "workload": f"{args.count} hexagonal diblock instances, grids 32^2..128^2, Ns 100, nhist 10, "
                         + ("nskip 5 nper 20, ftol=stol=1e-7" if args.sweep_domain else "fixed cells, ftol=1e-7"),
-            "precision": "fp32 then fp64 polish" if args.precision == "fp32" else "fp64",
+            "precision": "fp32 then fp64 polish" if args.precision == "fp32" else "fp64", "polish": args.polish,
             "n_ranks": world, "nthreads": args.nthreads, "wall_s": wall, "scft_iters_total": iters,
             "scft_iters_per_s": iters / wall, "converged": sum(1 for r in res if r["converged"]),
             "failed": sum(1 for r in res if r["status"] != 0),
@@ -442,6 +442,8 @@ def main():
     ap.add_argument("--count", type=int, default=256, help="sweep: instances")
     ap.add_argument("--nthreads", type=int, default=64, help="sweep: host threads")
     ap.add_argument("--sweep-domain", action="store_true", help="sweep: variable cells (DomainUpdater)")
+    ap.add_argument("--polish", default="auto", choices=["auto", "updater", "newton"],
+                    help="sweep: float64 phase of the mixed runs (SCFTOptions.polish)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

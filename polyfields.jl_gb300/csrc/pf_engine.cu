@@ -1123,11 +1123,12 @@ struct System {
   }
   // Pencil-pass autotuner.  The first time a 3D handle has solved a density for a transform
   // length and plane size that no handle of this process has tuned, each candidate schedule
-  // (pipeline stages x tiles per CTA) reruns the first kTuneSteps contour steps of the first
-  // chain (plane and pencil passes, as in a density solve; the rerun rewrites the same values),
-  // once untimed and once timed with CUDA events; the fastest is kept for every later launch.
-  // Schedules differ only in how tiles are distributed, not in arithmetic, so results do not
-  // depend on the choice.  PF_NO_AUTOTUNE=1 keeps the default schedule.
+  // (pipeline stages x tiles per CTA) reruns the first kTuneSteps contour steps of every chain
+  // on the chains' branch streams, as a density solve runs them (the rerun rewrites the same
+  // values), three times; the fastest of the last two timings (CUDA events) counts, and the
+  // fastest candidate is kept for every later launch.  Schedules differ only in how tiles are
+  // distributed, not in arithmetic, so results do not depend on the choice.  PF_NO_AUTOTUNE=1
+  // keeps the default schedule.
   bool autotune = true;
   cudaEvent_t tev[2] = {nullptr, nullptr};
   template <typename T>
@@ -1136,33 +1137,43 @@ struct System {
     const int nkp = (nx / 2 + 1) * ny;
     if (get_pencil_schedule<T>(nz, nkp, nullptr, nullptr)) return;
     static const int cands[][2] = {{2, 1}, {2, 2}, {3, 1}, {3, 2}, {3, 4}};
-    constexpr int kTuneSteps = 8;
-    ChainHost<T> h = hosts_of<T>()[0];
-    h.nsteps = std::min(kTuneSteps, h.nsteps);
+    constexpr int kTuneSteps = 16;
+    std::vector<ChainHost<T>> hs = hosts_of<T>();
+    int tsteps = 0;
+    for (auto& h : hs) {
+      h.nsteps = std::min(kTuneSteps, h.nsteps);
+      tsteps = std::max(tsteps, h.nsteps);
+    }
+    const Branches* brs = branches();
     for (auto& e : tev)
       if (!e) PF_CU(cudaEventCreate(&e));
     float best = 1e30f;
-    int bs = 0, br = 0;
+    int bs = 0, brd = 0;
     for (const auto& c : cands) {
-      h.zstages = c[0];
-      h.zrounds = c[1];
-      float ms = 0.0f;
-      for (int rep = 0; rep < 2; ++rep) {
+      for (auto& h : hs) {
+        h.zstages = c[0];
+        h.zrounds = c[1];
+      }
+      float tmin = 1e30f;
+      for (int rep = 0; rep < 3; ++rep) {
         PF_CU(cudaEventRecord(tev[0], st));
-        launch_chains<T>(jobs[p].as<ChainJob<T>>(), 1, h.nsteps, GridDims{nx, ny, nz}, tw<T>(p), st, &h);
+        launch_chains<T>(jobs[p].as<ChainJob<T>>(), njobs, tsteps, GridDims{nx, ny, nz}, tw<T>(p), st, hs.data(),
+                         brs);
         PF_CU(cudaEventRecord(tev[1], st));
         check_launch();
         PF_CU(cudaEventSynchronize(tev[1]));
+        float ms = 0.0f;
         PF_CU(cudaEventElapsedTime(&ms, tev[0], tev[1]));
+        if (rep > 0) tmin = std::min(tmin, ms);
       }
-      if (ms < best) {
-        best = ms;
+      if (tmin < best) {
+        best = tmin;
         bs = c[0];
-        br = c[1];
+        brd = c[1];
       }
     }
     check_pipe(p);
-    set_pencil_schedule<T>(nz, nkp, bs, br);
+    set_pencil_schedule<T>(nz, nkp, bs, brd);
   }
   void invalidate_graphs() {
     for (int p = 0; p < 2; ++p) {

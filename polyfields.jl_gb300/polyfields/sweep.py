@@ -35,7 +35,7 @@ def shard_by_cost(costs: Sequence[float], world: int) -> List[List[int]]:
 
 def run_local(params: Sequence[Dict], indices: Sequence[int], precision: str = "fp32", ftol: float = 1e-7,
               stol: float = 1e-7, switch: float = 1e-5, nsteps: int = 3000, nthreads: int = 0,
-              vcell: bool = True) -> Dict[int, Dict]:
+              vcell: bool = True, polish: str = "auto") -> Dict[int, Dict]:
     """Run the instances ``indices`` of ``params`` on this process's GPU with scft_batch:
     float32 iterations until ferr < ``switch`` then float64 polish to ``ftol``/``stol``
     (precision "fp32"), or float64 throughout ("fp64").  Returns {index: result dict}."""
@@ -49,7 +49,7 @@ def run_local(params: Sequence[Dict], indices: Sequence[int], precision: str = "
         ups.append(pf.AndersonUpdater(nhist=10))
         doms.append(pf.DomainUpdater(nskip=5, nper=20) if vcell else None)
     opts = pf.SCFTOptions(nsteps=nsteps, ftol=ftol, stol=stol,
-                          mixed_switch_ferr=switch if precision == "fp32" else 0.0)
+                          mixed_switch_ferr=switch if precision == "fp32" else 0.0, polish=polish)
     t0 = time.perf_counter()
     res, st = pf.scft_batch(systems, ups, doms if vcell else None, opts, nthreads=nthreads, raise_on_error=False)
     wall = time.perf_counter() - t0
