@@ -324,7 +324,7 @@ def run_gpu(args):
     return 0
 
 
-def tts_pair(n, seed, ftol=1e-8, nsteps=4000, switch=3e-6, nhist=NHIST):
+def tts_pair(n, seed, ftol=1e-8, nsteps=4000, switch=3e-3, nhist=NHIST):
     """Time to solution of the large blend on an n^3 grid (cell held at L0 = 14, seeded start):
     scft! with float64 propagators throughout, and the mixed path (float32 propagators until
     ferr < switch, then float64 polish), both to ftol.  Wall time of each pf_scft call."""
@@ -351,7 +351,7 @@ def tts_summary(n, seeds):
     runs = [dict(seed=sd, **tts_pair(n, sd)) for sd in seeds]
     ratios = sorted(r["wall_ratio"] for r in runs)
     return {"workload": f"large blend {n}^3 (cell held at L0 = 14), Anderson nhist {NHIST}, ftol 1e-8; mixed = "
-                        f"float32 propagators to ferr 3e-6, then Newton-Krylov polish (float64 residuals, "
+                        f"float32 propagators to ferr 3e-3, then Newton-Krylov polish (float64 residuals, "
                         f"float32 Jacobian products)",
             "seeds": list(seeds), "wall_ratio_median": statistics.median(ratios),
             "wall_ratio_min": ratios[0], "wall_ratio_max": ratios[-1],
@@ -389,9 +389,10 @@ def run_sweep(args):
     """Batched phase-diagram sweep of 2D hexagonal diblock instances (grids 32^2 .. 128^2, chiN ~
     U[12, 30], fA ~ U[0.25, 0.5], a0 ~ U[4, 9], Ns 100, seeded noise plus six-fold cosines; one
     seeded parameter stream): scft! with AndersonUpdater(nhist = 10), cells held fixed
-    (--sweep-domain: DomainUpdater(nskip = 5, nper = 20)), float32 until ferr < 1e-5 then
-    float64 polish to ftol = 1e-7 (--precision fp32) or float64 throughout.  Under torchrun the
-    instances are sharded over the ranks by cost and gathered on rank 0."""
+    (--sweep-domain: DomainUpdater(nskip = 5, nper = 20)), float32 until ferr < --switch
+    (1e-5) then float64 polish (--polish) to ftol = 1e-7 (--precision fp32) or float64
+    throughout.  Under torchrun the instances are sharded over the ranks by cost and gathered
+    on rank 0."""
     from polyfields import sweep as S
     from polyfields import workloads as W
     rank = int(os.environ.get("RANK", "0"))
@@ -404,7 +405,7 @@ def run_sweep(args):
     params = W.hex_sweep_params(args.count, 12345)
     t0 = time.perf_counter()
     res = S.run_sharded(params, rank, world, precision=args.precision, nsteps=3000, nthreads=args.nthreads,
-                        vcell=args.sweep_domain, polish=args.polish)
+                        vcell=args.sweep_domain, polish=args.polish, switch=args.switch)
     wall = time.perf_counter() - t0
     if rank == 0:
         iters = sum(r["iterations"] for r in res)
@@ -413,6 +414,7 @@ def run_sweep(args):
             "workload": f"{args.count} hexagonal diblock instances, grids 32^2..128^2, Ns 100, nhist 10, "
                         + ("nskip 5 nper 20, ftol=stol=1e-7" if args.sweep_domain else "fixed cells, ftol=1e-7"),
             "precision": "fp32 then fp64 polish" if args.precision == "fp32" else "fp64", "polish": args.polish,
+            "switch_ferr": args.switch,
             "n_ranks": world, "nthreads": args.nthreads, "wall_s": wall, "scft_iters_total": iters,
             "scft_iters_per_s": iters / wall, "converged": sum(1 for r in res if r["converged"]),
             "failed": sum(1 for r in res if r["status"] != 0),
@@ -444,6 +446,7 @@ def main():
     ap.add_argument("--sweep-domain", action="store_true", help="sweep: variable cells (DomainUpdater)")
     ap.add_argument("--polish", default="auto", choices=["auto", "updater", "newton"],
                     help="sweep: float64 phase of the mixed runs (SCFTOptions.polish)")
+    ap.add_argument("--switch", type=float, default=1e-5, help="sweep: ferr at which the mixed runs switch to float64")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
