@@ -1512,13 +1512,21 @@ struct System {
   // with float64 propagators): w <- w + delta with J delta = -F64(w) solved by restarted GMRES
   // whose Jacobian-vector products are finite differences of float32 residuals about w,
   //   J v ~ (F32(w + e v) - F32(w)) / e,   e |v| = kNKStep |w|.
-  // A perturbation of 1% of the field keeps float32 rounding (ferr ~ 1e-6 of |w|) below 1e-3
-  // of each product, which is accurate enough for Newton steps that each shrink ferr by a
-  // factor ~20-50; only the acceptance test and the right-hand side are float64 solves.  The
-  // fixed point is the reference's: a run ends only when the float64 ferr < ftol.
+  // A perturbation of 0.1% of the field balances the two errors of a product: float32 rounding
+  // (~1e-7 of |w| in the residual, ~1e-4 of the product) and the one-sided difference's
+  // truncation (~1e-3 of it; at 1% the truncation limited each Newton step to shrinking ferr
+  // 6-10x and the GMRES solves to 1e-2 were largely wasted).  Only the acceptance test and the
+  // right-hand side are float64 solves.  The forcing term (the GMRES tolerance relative to
+  // |F64|) is 0.3 far from the answer and no tighter than kNKEtaMin: tighter solves buy no more
+  // per Newton step than the finite-difference Jacobian allows (at 0.1 a 128^3 run stalled and
+  // fell back to float64 updater steps).  Measured on the 128^3 blend from a switch at ferr
+  // 3e-3: 221 float32 products and 5 float64 residuals (4.5 s) against 290 and 6 (5.4 s) with a
+  // 1% step and a floor of 1e-2.  The fixed point is the reference's: a run ends only when the
+  // float64 ferr < ftol.
   static constexpr int kNKRestart = 30;      // GMRES restart length
   static constexpr int kNKMaxMatvec = 240;   // float32 products per Newton step at most
-  static constexpr double kNKStep = 1e-2;
+  static constexpr double kNKStep = 1e-3;
+  static constexpr double kNKEtaMin = 3e-2;
   struct NKBufs {
     DevBuf V, wk, r64, r32, z, delta, h, part;
   } nkb;
@@ -1577,7 +1585,7 @@ struct System {
       residuals();
       PF_CU(cudaMemcpyAsync(nkb.r32.p, res.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
       ++nk_fp32;
-      const double eta = std::min(0.3, std::max(1e-2, 0.3 * o.ftol / ferr));  // forcing term
+      const double eta = std::min(0.3, std::max(kNKEtaMin, 0.3 * o.ftol / ferr));  // forcing term
       PF_CU(cudaMemsetAsync(delta, 0, sizeof(double) * n, st));
       // first cycle: V_0 = -r64 / beta
       PF_CU(cudaMemcpyAsync(V, r64, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
