@@ -179,6 +179,47 @@ def run_reference(args):
     return 0
 
 
+def replica_env():
+    """(rank, world) of this process under torchrun (1 GPU per rank), else (0, 1)."""
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+
+
+def pin_replica_gpu():
+    """Under torchrun with several ranks, make this rank see only its own GPU (LOCAL_RANK-th of
+    the visible ones) before CUDA starts: every rank then runs one independent instance on its
+    device 0 (a single SCFT instance does not shard: each contour step is a full 3D FFT)."""
+    rank, world = replica_env()
+    if world <= 1:
+        return
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    devs = [d for d in vis.split(",") if d.strip()] if vis else None
+    os.environ["CUDA_VISIBLE_DEVICES"] = devs[local % len(devs)] if devs else str(local)
+
+
+def replica_group():
+    """Host process group (gloo) of the replicas, or None when running alone."""
+    rank, world = replica_env()
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group("gloo")
+    return dist
+
+
+def aggregate_replicas(dist, ms_total, units):
+    """Whole-job rate of `units` per rank over the slowest rank's time: (world * units) /
+    max(ms_total) per second, and that max (ms).  dist None: one rank."""
+    if dist is None:
+        return 1000.0 * units / ms_total, ms_total
+    import torch
+    t = torch.tensor([float(ms_total)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    mx = float(t.item())
+    return 1000.0 * units * dist.get_world_size() / mx, mx
+
+
 def run_gpu(args):
     import numpy as np
     import polyfields as pf
@@ -186,8 +227,10 @@ def run_gpu(args):
     from polyfields.workloads import blend3d_system
 
     lib = L.load()
-    if args.gpus != 1:
-        raise SystemExit("the engine runs one SCFT instance per GPU; run with --gpus 1")
+    rank, world = replica_env()
+    if args.gpus != world:
+        raise SystemExit(f"--gpus {args.gpus} but {world} rank(s): launch N ranks with torchrun for --gpus N")
+    dist = replica_group()  # N > 1: N independent replicas (no data-path collective)
     n = args.size
     sysm = blend3d_system(pf, n=n, precision="fp32")
     ng = n ** 3
@@ -207,7 +250,10 @@ def run_gpu(args):
 
     # ---- timed region: K scft! iterations with FP32 propagators
     clocks = ClockSampler()
-    clocks.start()
+    if rank == 0:
+        clocks.start()
+    if dist is not None:
+        dist.barrier()
     l0 = lib.pf_launch_count()
     prop_ms = 0.0
     dens_ms = 0.0
@@ -224,9 +270,9 @@ def run_gpu(args):
     L.check(lib.pf_elapsed_ms(sysm._h, 0, 1, ctypes.byref(ms)), sysm._h)
     t_host = time.perf_counter() - t_host
     launches = lib.pf_launch_count() - l0
-    clk = clocks.stop()
-    ms_per_step = ms.value / args.steps
-    value = 1000.0 / ms_per_step
+    clk = clocks.stop() if rank == 0 else None
+    value, ms_max = aggregate_replicas(dist, ms.value, args.steps)
+    ms_per_step = ms_max / args.steps
     prop_step_ms = prop_ms / args.steps
     mde_step_us = 1000.0 * prop_step_ms / nmde
     ferr = sysm.field_error()
@@ -265,6 +311,8 @@ def run_gpu(args):
         host[m][...] = sysm.fields[m]
     e2e_steps = max(1, min(args.steps, 5))
     sysm.synchronize()
+    if dist is not None:
+        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         for m in (1, 2):
@@ -273,13 +321,17 @@ def run_gpu(args):
         for m in (1, 2):
             L.check(lib.pf_get_grid(sysm._h, L.PF_FIELD, m, L.dptr(host[m])), sysm._h)
         _ = sysm.free_energy()
-    e2e_dt = (time.perf_counter() - t0) / e2e_steps
-    e2e = {"value": 1.0 / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * ng, "d2h_bytes_per_step": 2 * 8 * ng + 8,
+    e2e_value, _ = aggregate_replicas(dist, 1000.0 * (time.perf_counter() - t0), e2e_steps)
+    e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": world * 2 * 8 * ng,
+           "d2h_bytes_per_step": world * (2 * 8 * ng + 8),
            "api": "pf_set_field x2 + pf_anderson_step + pf_get_grid x2 + pf_free_energy"}
+    if rank != 0:
+        return 0
 
-    # ---- FP64 propagators on the same state (the plain FP64 GPU solver's iteration rate)
+    # ---- FP64 propagators on the same state (the plain FP64 GPU solver's iteration rate; one
+    # GPU, so only when the benchmark runs alone)
     fp64 = None
-    if args.fp64_steps > 0:
+    if args.fp64_steps > 0 and world == 1:
         sysm.precision = "fp64"
         upd.step()
         L.check(lib.pf_record_event(sysm._h, 2), sysm._h)
@@ -306,13 +358,16 @@ def run_gpu(args):
             _ = sysm.free_energy()
         fp64["e2e_iters_per_s"] = e2e_steps / (time.perf_counter() - t0)
 
-    cpu = cpu_baseline_sample() if args.cpu_seconds > 0 else None
+    # the CPU baseline and the time to solution run with the benchmark alone (N = 1)
+    cpu = cpu_baseline_sample() if args.cpu_seconds > 0 and world == 1 else None
     del upd, sysm
     # time to solution, mixed vs plain FP64, on a grid that fits the run's time (median of seeds)
-    tts = tts_summary(args.tts_size, [12345 + 1000 * i for i in range(args.seeds)]) if args.tts_size > 0 else None
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+    tts = (tts_summary(args.tts_size, [12345 + 1000 * i for i in range(args.seeds)])
+           if args.tts_size > 0 and world == 1 else None)
+    config = dict(WORKLOAD, size=n, parallelism=("replicas: one independent instance per GPU" if world > 1 else "1 GPU"))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 propagators + f64 reductions", "data": "synthetic", "config": dict(WORKLOAD, size=n),
+            "dtype": "f32 propagators + f64 reductions", "data": "synthetic", "config": config,
             "mde_steps_per_s": value * nmde, "mde_steps_per_iter": nmde, "propagate_ms_per_iter": prop_step_ms,
             "density_ms_per_iter": dens_ms / args.steps, "host_ms_per_step": 1000.0 * t_host / args.steps,
             "fp64": fp64, "mixed_vs_fp64_iter_speedup": (value / fp64["iters_per_s"]) if fp64 else None,
@@ -397,10 +452,8 @@ def run_sweep(args):
     from polyfields import workloads as W
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    if world > 1:
-        import torch
+    if world > 1:  # each rank sees only its own GPU (pin_replica_gpu)
         import torch.distributed as dist
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("gloo")
     params = W.hex_sweep_params(args.count, 12345)
     t0 = time.perf_counter()
@@ -460,4 +513,6 @@ def main():
 
 
 if __name__ == "__main__":
+    if "--impl" not in sys.argv:
+        pin_replica_gpu()
     sys.exit(main())
