@@ -1433,6 +1433,8 @@ struct System {
       fprintf(stderr, "Warning: Using previous iterations in AndersonUpdater history.\n");
       return;
     }
+    if (ensemble != 0)  // anderson.jl:61-63
+      throw PFError(E_STATE, "Anderson mixing can only be used for systems in the canonical ensemble.");
     const size_t slot = sizeof(double) * nmon() * ng;
     and_.res_hist.alloc(slot * (and_.nhist + 1));
     and_.field_hist.alloc(slot * (and_.nhist + 1));

@@ -400,3 +400,23 @@ def test_pencil_schedule_is_autotuned_on_first_solve():
     assert g.species[0].Q == pytest.approx(o.species[0].Q, rel=FP32_RTOL)
     for mid in (1, 2):
         assert rel(g.density[mid], o.density[mid]) < FP32_RTOL
+
+
+def test_anderson_rejects_the_grand_ensemble():
+    """AndersonUpdater setup! (anderson.jl:61-63) refuses a Grand-ensemble system with the
+    reference's message, as the oracle does."""
+    def build(M):
+        A, B = M.Monomer(1, 1.0), M.Monomer(2, 1.0)
+        ens = O.GRAND if M is O else pf.Grand
+        s = M.FieldSystem((32, 1, 1), M.UnitCell(1, "lamellar", 8.0), monomers=[A, B], ensemble=ens)
+        s.add_species(M.Diblock(A, B, 100, 0.5, 1.0, 1.0, 100), -1.0)
+        f = M.FloryInteraction()
+        f.set_interaction(A, B, 0.2)
+        s.add_interaction(f)
+        M.fieldinit(s, SY.seeded_fields((1, 1, 32), [1, 2], 7, 0.3))
+        return s
+    msg = "Anderson mixing can only be used for systems in the canonical ensemble."
+    with pytest.raises(ValueError, match=msg):
+        O.scft(build(O), O.AndersonUpdater(nhist=5), opts=O.SCFTOptions(nsteps=3))
+    with pytest.raises(pf.PolyFieldsError, match=msg):
+        pf.scft(build(pf), pf.AndersonUpdater(nhist=5), opts=pf.SCFTOptions(nsteps=3))
