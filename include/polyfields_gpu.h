@@ -160,14 +160,22 @@ int pf_anderson_setup(pf_system* sys);
 /* step!(::AndersonUpdater) (src/updaters/anderson.jl:98-228) */
 int pf_anderson_step(pf_system* sys);
 /* EulerUpdater(; method = :PECE, lam = 0.05) (src/updaters/euler.jl:9-29): method 0 = :PEC,
- * 1 = :PECE.  Becomes the handle's field updater (replacing an AndersonUpdater). */
+ * 1 = :PECE.  Adds an updater with its own state to the handle and makes it current. */
 int pf_euler_create(pf_system* sys, int method, double lam);
 /* MomentumUpdater(; method = :MOM, lam = 0.01, gamma = 0.9, beta1 = 0.9, beta2 = 0.999)
- * (src/updaters/momentum.jl:19-47): method 0 = :MOM, 1 = :RMS, 2 = :ADAM, 3 = :NAG.  Becomes
- * the handle's field updater. */
+ * (src/updaters/momentum.jl:19-47): method 0 = :MOM, 1 = :RMS, 2 = :ADAM, 3 = :NAG.  Adds an
+ * updater with its own state to the handle and makes it current. */
 int pf_momentum_create(pf_system* sys, int method, double lam, double gamma, double beta1, double beta2);
-/* setup!(updater, sys) / step!(updater) for the field updater created last (Anderson, Euler
- * or Momentum): src/updaters/base.jl:7-9 dispatch. */
+/* Several updaters on one system, as the reference's updater objects allow
+ * (test/test_updaters.jl:16-30 sets up an Euler, a NAG and an Anderson updater on one system,
+ * then steps each in turn).  pf_updater_current writes the id of the current updater (-1: the
+ * Anderson updater; 0, 1, ...: the Euler/Momentum updaters in creation order);
+ * pf_updater_select makes one current again (PF_EARG for an unknown id, PF_ESTATE for -1
+ * without an Anderson updater).  Their device state lives until pf_system_destroy. */
+int pf_updater_current(pf_system* sys, int* id);
+int pf_updater_select(pf_system* sys, int id);
+/* setup!(updater, sys) / step!(updater) for the current field updater (Anderson, Euler or
+ * Momentum): src/updaters/base.jl:7-9 dispatch. */
 int pf_updater_setup(pf_system* sys);
 int pf_updater_step(pf_system* sys);
 /* DomainUpdater(; nper = 10, nskip = 200, lam = 0.1, pmax = 1.0, rlxn = 0.5) (src/updaters/domain.jl:20-24) */
@@ -179,8 +187,8 @@ int pf_domain_step(pf_system* sys, int nsteps);
 /* stress_error(domain) (src/updaters/domain.jl:30) */
 int pf_domain_stress_error(pf_system* sys, double* out);
 
-/* scft!(sys, updater; domain, opts) (src/simulate.jl:60-148) with the field updater created
- * last (pf_anderson_create, pf_euler_create or pf_momentum_create; required) and the
+/* scft!(sys, updater; domain, opts) (src/simulate.jl:60-148) with the current field updater
+ * (pf_anderson_create, pf_euler_create, pf_momentum_create or pf_updater_select; required) and the
  * DomainUpdater of pf_domain_create (used when use_domain != 0). */
 int pf_scft(pf_system* sys, const pf_scft_options* opts, int use_domain, pf_scft_results* out);
 

@@ -525,7 +525,10 @@ struct System {
     }
   } and_;
   // EulerUpdater (kind 1, method 0 PEC / 1 PECE) and MomentumUpdater (kind 2, method 0 MOM,
-  // 1 RMS, 2 ADAM, 3 NAG); `active` is the kind of the updater created last (0 = Anderson)
+  // 1 RMS, 2 ADAM, 3 NAG).  A system can carry several of them, each with its own state, as
+  // the reference's updater objects do (test/test_updaters.jl:16-30 sets up an Euler, a NAG
+  // and an Anderson updater on one system and steps each in turn).  `su` is the current one;
+  // `active` is the kind of the current updater (0 = the Anderson updater).
   struct SimpleUpdater {
     int kind = 0, method = 0;
     bool is_setup = false;
@@ -542,7 +545,9 @@ struct System {
       mt.release();
       vt.release();
     }
-  } su;
+  };
+  std::vector<std::unique_ptr<SimpleUpdater>> simple;
+  SimpleUpdater* su = nullptr;
   int active = 0;
   // Domain updater (src/updaters/domain.jl:7-24)
   struct Domain {
@@ -1453,35 +1458,36 @@ struct System {
 
   // ---------------------------------------------------------------- Euler / Momentum
   void simple_setup() {  // euler.jl:31-35, momentum.jl:49-61
+    if (!su) throw PFError(E_STATE, "no field updater created");
     const long nall = (long)nmon() * ng;
-    su.temp.alloc(sizeof(double) * nall);
-    PF_CU(cudaMemcpyAsync(su.temp.p, w.p, sizeof(double) * nall, cudaMemcpyDeviceToDevice, st));
-    if (su.kind == 2) {
-      su.mt.alloc(sizeof(double) * nall);
-      su.vt.alloc(sizeof(double) * nall);
-      PF_CU(cudaMemsetAsync(su.mt.p, 0, su.mt.bytes, st));
-      PF_CU(cudaMemsetAsync(su.vt.p, 0, su.vt.bytes, st));
+    su->temp.alloc(sizeof(double) * nall);
+    PF_CU(cudaMemcpyAsync(su->temp.p, w.p, sizeof(double) * nall, cudaMemcpyDeviceToDevice, st));
+    if (su->kind == 2) {
+      su->mt.alloc(sizeof(double) * nall);
+      su->vt.alloc(sizeof(double) * nall);
+      PF_CU(cudaMemsetAsync(su->mt.p, 0, su->mt.bytes, st));
+      PF_CU(cudaMemsetAsync(su->vt.p, 0, su->vt.bytes, st));
     }
-    su.is_setup = true;
+    su->is_setup = true;
   }
   void simple_step() {  // euler.jl:37-65, momentum.jl:63-165
-    if (!su.is_setup) throw PFError(E_STATE, "field updater not set up");
+    if (!su || !su->is_setup) throw PFError(E_STATE, "field updater not set up");
     const long nall = (long)nmon() * ng;
     double* wp = w.as<double>();
     double* rp = res.as<double>();
-    double* tp = su.temp.as<double>();
-    if (su.kind == 1) {
-      launch_euler_predict(wp, tp, rp, su.lam, nall, st);
+    double* tp = su->temp.as<double>();
+    if (su->kind == 1) {
+      launch_euler_predict(wp, tp, rp, su->lam, nall, st);
       residuals();
-      launch_euler_correct(wp, tp, rp, su.lam, nall, st);
-      if (su.method == 1) residuals();
-    } else if (su.method == 3) {
-      launch_nag_ahead(wp, tp, su.mt.as<double>(), su.lam, nall, st);
+      launch_euler_correct(wp, tp, rp, su->lam, nall, st);
+      if (su->method == 1) residuals();
+    } else if (su->method == 3) {
+      launch_nag_ahead(wp, tp, su->mt.as<double>(), su->lam, nall, st);
       residuals();
-      launch_nag_update(wp, tp, su.mt.as<double>(), rp, su.lam, su.gamma, nall, st);
+      launch_nag_update(wp, tp, su->mt.as<double>(), rp, su->lam, su->gamma, nall, st);
     } else {
       residuals();
-      launch_momentum(su.method, wp, su.mt.as<double>(), su.vt.as<double>(), rp, su.lam, su.beta1, su.beta2, nall,
+      launch_momentum(su->method, wp, su->mt.as<double>(), su->vt.as<double>(), rp, su->lam, su->beta1, su->beta2, nall,
                       st);
     }
     check_launch();
@@ -2601,7 +2607,9 @@ int pf_euler_create(pf_system* sys, int method, double lam) {
   return guard(sys, [&](pf::System& s) {
     if (method != 0 && method != 1)
       throw pf::PFError(PF_EARG, "Invalid `method` parameter for EulerUpdater. Options include: (:PEC, :PECE)");
-    s.su.reset(1, method, lam);
+    s.simple.push_back(std::make_unique<pf::System::SimpleUpdater>());
+    s.su = s.simple.back().get();
+    s.su->reset(1, method, lam);
     s.active = 1;
   });
 }
@@ -2612,11 +2620,34 @@ int pf_momentum_create(pf_system* sys, int method, double lam, double gamma, dou
                         "Invalid `method` parameter for MomentumUpdater. Options include: (:MOM, :RMS, :ADAM, :NAG)");
     if (!(gamma > 0.0 && gamma < 1.0) || !(beta1 > 0.0 && beta1 < 1.0) || !(beta2 > 0.0 && beta2 < 1.0))
       throw pf::PFError(PF_EARG, "AssertionError: 0 < gamma, beta1, beta2 < 1");
-    s.su.reset(2, method, lam);
-    s.su.gamma = gamma;
-    s.su.beta1 = beta1;
-    s.su.beta2 = beta2;
+    s.simple.push_back(std::make_unique<pf::System::SimpleUpdater>());
+    s.su = s.simple.back().get();
+    s.su->reset(2, method, lam);
+    s.su->gamma = gamma;
+    s.su->beta1 = beta1;
+    s.su->beta2 = beta2;
     s.active = 2;
+  });
+}
+int pf_updater_current(pf_system* sys, int* id) {
+  return guard(sys, [&](pf::System& s) {
+    if (!id) throw pf::PFError(PF_EARG, "null output pointer");
+    *id = -1;
+    if (s.active != 0)
+      for (size_t i = 0; i < s.simple.size(); ++i)
+        if (s.simple[i].get() == s.su) *id = (int)i;
+  });
+}
+int pf_updater_select(pf_system* sys, int id) {
+  return guard(sys, [&](pf::System& s) {
+    if (id == -1) {
+      if (!s.and_.exists) throw pf::PFError(PF_ESTATE, "no AndersonUpdater created");
+      s.active = 0;
+      return;
+    }
+    if (id < 0 || id >= (int)s.simple.size()) throw pf::PFError(PF_EARG, "no field updater with this id");
+    s.su = s.simple[id].get();
+    s.active = s.su->kind;
   });
 }
 int pf_updater_setup(pf_system* sys) { return guard(sys, [&](pf::System& s) { s.updater_setup(); }); }

@@ -75,6 +75,8 @@ SIGNATURES = {
     "pf_euler_create": (_c_int, [_vp, _c_int, ctypes.c_double]),
     "pf_momentum_create": (_c_int, [_vp, _c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double]),
+    "pf_updater_current": (_c_int, [_vp, ctypes.POINTER(_c_int)]),
+    "pf_updater_select": (_c_int, [_vp, _c_int]),
     "pf_updater_setup": (_c_int, [_vp]),
     "pf_updater_step": (_c_int, [_vp]),
     "pf_set_density_cotangent": (_c_int, [_vp, _c_int, _dptr]),

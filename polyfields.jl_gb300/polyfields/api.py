@@ -555,9 +555,12 @@ class AndersonUpdater:
         self.system: Optional[FieldSystem] = None
 
     def _bind(self, sys: FieldSystem) -> None:
+        """Create the updater's history on sys (once per system) and make it the current one."""
         if self.system is not sys:
             L.check(L.load().pf_anderson_create(sys._h, self.nhist, self.iter_euler, self.lam_euler), sys._h)
             self.system = sys
+        else:
+            L.check(L.load().pf_updater_select(sys._h, -1), sys._h)
 
     def setup(self, sys: FieldSystem) -> None:
         """setup!(updater, sys) — anderson.jl:54-92."""
@@ -571,7 +574,41 @@ class AndersonUpdater:
         L.check(L.load().pf_anderson_step(self.system._h), self.system._h)
 
 
-class EulerUpdater:
+class _SimpleUpdater:
+    """State of an Euler or Momentum updater on the device of its system.  Each updater object
+    owns its own state there (created on first use with a system), so several updaters can be
+    set up on one system and stepped in turn, as test/test_updaters.jl:16-30 does."""
+
+    system: Optional[FieldSystem] = None
+    _id: int = -1
+
+    def _create(self, sys: FieldSystem) -> None:
+        raise NotImplementedError
+
+    def _bind(self, sys: FieldSystem) -> None:
+        lib = L.load()
+        if self.system is not sys:
+            self._create(sys)
+            uid = ctypes.c_int()
+            L.check(lib.pf_updater_current(sys._h, ctypes.byref(uid)), sys._h)
+            self.system, self._id = sys, uid.value
+        else:
+            L.check(lib.pf_updater_select(sys._h, self._id), sys._h)
+
+    def setup(self, sys: FieldSystem) -> None:
+        """setup!(updater, sys) — euler.jl:31-35, momentum.jl:49-61."""
+        self._bind(sys)
+        L.check(L.load().pf_updater_setup(sys._h), sys._h)
+
+    def step(self) -> None:
+        """step!(updater) — euler.jl:37-65, momentum.jl:63-165."""
+        if self.system is None:
+            raise RuntimeError(f"{type(self).__name__} is not set up")
+        self._bind(self.system)
+        L.check(L.load().pf_updater_step(self.system._h), self.system._h)
+
+
+class EulerUpdater(_SimpleUpdater):
     """EulerUpdater(; method = :PECE, lam = 0.05) — euler.jl:9-29 (predictor-corrector Euler)."""
 
     _METHODS = {"PEC": 0, "PECE": 1}
@@ -583,21 +620,11 @@ class EulerUpdater:
         self.method, self.lam = method, float(lam)
         self.system: Optional[FieldSystem] = None
 
-    def _bind(self, sys: FieldSystem) -> None:
+    def _create(self, sys: FieldSystem) -> None:
         L.check(L.load().pf_euler_create(sys._h, self._METHODS[self.method], self.lam), sys._h)
-        self.system = sys
-
-    def setup(self, sys: FieldSystem) -> None:
-        self._bind(sys)
-        L.check(L.load().pf_updater_setup(sys._h), sys._h)
-
-    def step(self) -> None:
-        if self.system is None:
-            raise RuntimeError("EulerUpdater is not set up")
-        L.check(L.load().pf_updater_step(self.system._h), self.system._h)
 
 
-class MomentumUpdater:
+class MomentumUpdater(_SimpleUpdater):
     """MomentumUpdater(; method = :MOM, lam = 0.01, gamma = 0.9, beta1 = 0.9, beta2 = 0.999)
     — momentum.jl:19-47 (MOM, RMS, ADAM, NAG)."""
 
@@ -613,19 +640,9 @@ class MomentumUpdater:
         self.gamma, self.beta1, self.beta2 = float(gamma), float(beta1), float(beta2)
         self.system: Optional[FieldSystem] = None
 
-    def _bind(self, sys: FieldSystem) -> None:
+    def _create(self, sys: FieldSystem) -> None:
         L.check(L.load().pf_momentum_create(sys._h, self._METHODS[self.method], self.lam, self.gamma, self.beta1,
                                             self.beta2), sys._h)
-        self.system = sys
-
-    def setup(self, sys: FieldSystem) -> None:
-        self._bind(sys)
-        L.check(L.load().pf_updater_setup(sys._h), sys._h)
-
-    def step(self) -> None:
-        if self.system is None:
-            raise RuntimeError("MomentumUpdater is not set up")
-        L.check(L.load().pf_updater_step(self.system._h), self.system._h)
 
 
 class DomainUpdater:

@@ -160,3 +160,39 @@ def bcc_system(M, n=64, L=7.0, precision=None, Ns=100, seed=12345):
     wa = 0.1 * rng.standard_normal(shape) + pat / 4.0
     M.fieldinit(sys, {1: wa, 2: -wa})
     return sys
+
+
+def _julia_seed_fields(case):
+    d = np.load(os.path.join(GOLDEN, "julia_seed_fields.npz"))
+    pre = f"{case}_w"
+    return {int(k[len(pre):]): d[k] for k in d.files if k.startswith(pre)}
+
+
+def reference_test_system(M, precision=None):
+    """test/test_system.jl:3-26: 32x1x1 lamellar (L 10), Point(C) phi 0.75 + Diblock(A, B, N100,
+    f0.5, Ns100) phi 0.25, chi_AB 0.2, with the fields of fieldinit!(sys; scale = 0.1,
+    seed = 12345) (the Julia randn stream, fixture julia_seed_fields.npz).  Returns
+    (sys, point, chain)."""
+    A, B, C = M.Monomer(1, 1.0, 0.0), M.Monomer(2, 1.0, 0.0), M.Monomer(3, 1.0, 0.0)
+    point = M.Point(C)
+    chain = M.Diblock(A, B, 100, 0.5, 1.0, 1.0, 100)
+    itx = M.FloryInteraction()
+    itx.set_interaction(A, B, 0.2)
+    sys = _fs(M, (32, 1, 1), M.UnitCell(1, "lamellar", 10.0), [A, B, C], precision)
+    sys.add_species(point, 0.75)
+    sys.add_species(chain, 0.25)
+    sys.add_interaction(itx)
+    M.fieldinit(sys, _julia_seed_fields("system"))
+    return sys, point, chain
+
+
+def reference_test_updaters_system(M, precision=None):
+    """test/test_updaters.jl:3-14: the same diblock alone (phi 1), same seeded fields."""
+    A, B = M.Monomer(1, 1.0, 0.0), M.Monomer(2, 1.0, 0.0)
+    itx = M.FloryInteraction()
+    itx.set_interaction(A, B, 0.2)
+    sys = _fs(M, (32, 1, 1), M.UnitCell(1, "lamellar", 10.0), [A, B], precision)
+    sys.add_species(M.Diblock(A, B, 100, 0.5, 1.0, 1.0, 100), 1.0)
+    sys.add_interaction(itx)
+    M.fieldinit(sys, _julia_seed_fields("updaters"))
+    return sys

@@ -54,3 +54,26 @@ CYL2D_FINAL_128 = {"ferr": 9.910317272221094e-6, "fhelm": 0.10659231121049459,
 # 0.25, L = 13.100000015310233 (seed examples/seeds/lam1d.json is 64x1x1); converged at
 # step 0.
 LAM1D_FINAL_128 = {"ferr": 9.713161299981836e-6, "fhelm": 0.10211268214323928}
+
+# test/test_system.jl:3-34 — 32x1x1 lamellar (L 10), Point(C) phi 0.75 + Diblock(A, B, N100,
+# f0.5, b 1, 1, Ns100) phi 0.25, chi_AB 0.2, fieldinit!(sys; scale = 0.1, seed = 12345), then
+# density!(point), density!(chain).  The fields are Julia's seeded randn stream, restated in
+# oracle/julia_rng.py (fixture tests/golden/julia_seed_fields.npz, keys system_w*).
+TEST_SYSTEM = {
+    "point_Q": 1.004177455788938,
+    "chain_Q": 8.24300700515971,
+    "free_energy": -0.1681580628744596,
+    "free_energy_bulk": -0.9686022902416352,
+    "scfstress_1": -0.0004272750367130805,
+}
+
+# test/test_updaters.jl:3-30 — the same diblock alone (phi 1) with the same fieldinit!; an
+# EulerUpdater(:PECE, lam 0.005), a MomentumUpdater(:NAG, lam 0.005) and an
+# AndersonUpdater(nhist 5) are all set up first, then each takes 10 steps in that order
+# (fixture keys updaters_w*).  free_energy after the Euler steps (:24) and after the
+# Anderson steps (:30); the value after the NAG steps is the file's commented-out check (:27).
+TEST_UPDATERS = {
+    "after_euler": 0.0626842750325202,
+    "after_nag_commented_out": 0.06172669754976512,
+    "after_anderson": 0.12798422498635653,
+}

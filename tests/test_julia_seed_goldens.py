@@ -1,0 +1,86 @@
+"""The reference's RNG-dependent test goldens, pinned on the oracle.
+
+test/test_system.jl and test/test_updaters.jl start from `fieldinit!(sys; scale = 0.1,
+seed = 12345)`, i.e. Julia's seeded `randn` stream.  oracle/julia_rng.py restates that stream
+(dSFMT-19937 MersenneTwister, ziggurat randn, Dict order), the fixture
+tests/golden/julia_seed_fields.npz holds its output, and the FP64 oracle evaluated on those
+fields must give the numbers the reference's tests assert.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import julia_rng as J
+import pf_oracle as O
+import reference_values as RV
+from polyfields import workloads as W
+
+
+def test_mersenne_twister_matches_julias_documented_draws():
+    """Julia's manual: `Random.seed!(1234); rand()` (the `seed!` docstring) and
+    `randn(MersenneTwister(1234), ComplexF64)` = 0.6133070881429037 - 0.6376291670853887im,
+    i.e. two randn draws scaled by 1/sqrt(2)."""
+    rng = J.MersenneTwister(1234)
+    assert rng.rand() == 0.5908446386657102
+    pytest.importorskip("mpmath")
+    rng = J.MersenneTwister(1234)
+    re, im = J.randn(rng), J.randn(rng)
+    assert re == 0.8673472019512456
+    assert im == -0.9017438158568171
+    assert re / math.sqrt(2) == pytest.approx(0.6133070881429037, rel=1e-15)
+    assert im / math.sqrt(2) == pytest.approx(-0.6376291670853887, rel=1e-15)
+
+
+def test_dict_iteration_order_of_monomer_ids():
+    assert J.dict_order([1, 2, 3]) == [2, 3, 1]
+    assert J.dict_order([1, 2]) == [2, 1]
+    assert J.dict_order([3, 1, 2]) == [2, 3, 1]   # insertion order does not matter without collisions
+
+
+def test_fixture_is_what_the_restatement_draws():
+    pytest.importorskip("mpmath")
+    import make_julia_seed_fields as MK
+    fresh = MK.fields()
+    d = np.load(f"{W.GOLDEN}/julia_seed_fields.npz")
+    assert sorted(d.files) == sorted(fresh)
+    for k in d.files:
+        assert np.array_equal(d[k], fresh[k]), k
+
+
+def test_oracle_reproduces_test_system_goldens():
+    """test/test_system.jl:29-34 (`@test ... ≈ ...`, rtol sqrt(eps)); the oracle matches to a
+    few ulps."""
+    sys, point, chain = W.reference_test_system(O)
+    point.density_update()
+    chain.density_update()
+    g = RV.TEST_SYSTEM
+    assert point.Q == pytest.approx(g["point_Q"], rel=1e-14)
+    assert chain.Q == pytest.approx(g["chain_Q"], rel=1e-14)
+    assert sys.free_energy() == pytest.approx(g["free_energy"], rel=1e-14)
+    assert sys.free_energy_bulk() == pytest.approx(g["free_energy_bulk"], rel=1e-14)
+    assert sys.scfstress()[0] == pytest.approx(g["scfstress_1"], rel=1e-14)
+
+
+def test_oracle_reproduces_test_updaters_goldens():
+    """test/test_updaters.jl:18-30: Euler, NAG and Anderson updaters set up on one system,
+    then 10 steps of each in turn.  Euler and NAG to a few ulps; Anderson within the
+    reference test's own tolerance (its Gram solve amplifies last-bit FFT differences)."""
+    sys = W.reference_test_updaters_system(O)
+    u1 = O.EulerUpdater(method="PECE", lam=0.005)
+    u1.setup(sys)
+    u2 = O.MomentumUpdater(method="NAG", lam=0.005)
+    u2.setup(sys)
+    u3 = O.AndersonUpdater(nhist=5)
+    u3.setup(sys)
+    g = RV.TEST_UPDATERS
+    for _ in range(10):
+        u1.step()
+    assert sys.free_energy() == pytest.approx(g["after_euler"], rel=1e-14)
+    for _ in range(10):
+        u2.step()
+    assert sys.free_energy() == pytest.approx(g["after_nag_commented_out"], rel=1e-14)
+    for _ in range(10):
+        u3.step()
+    assert sys.free_energy() == pytest.approx(g["after_anderson"], rel=1e-9)
+    assert sys.free_energy() == pytest.approx(g["after_anderson"], rel=math.sqrt(np.finfo(float).eps))
