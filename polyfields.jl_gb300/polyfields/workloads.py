@@ -196,3 +196,21 @@ def reference_test_updaters_system(M, precision=None):
     sys.add_interaction(itx)
     M.fieldinit(sys, _julia_seed_fields("updaters"))
     return sys
+
+
+def notebook_blend_seeded_system(M, precision=None):
+    """examples/examples.ipynb cell 11: the ABC blend (Point C vol 1 phi 0.4, homopolymers A, B
+    vol 2 N100 phi 0.3 each; chi_AB 0.5, chi_AC = chi_BC = 1.25) on 256x1x1 (L 20), with the
+    fields of fieldinit!(sys; scale = 0.05, seed = 12345) (fixture julia_seed_fields.npz)."""
+    A, B, C = M.Monomer(1, 2.0), M.Monomer(2, 2.0), M.Monomer(3, 1.0)
+    sys = _fs(M, (256, 1, 1), M.UnitCell(1, "lamellar", 20.0), [A, B, C], precision)
+    sys.add_species(M.Point(C), 0.4)
+    sys.add_species(M.Homopolymer(A, 100, 1.0), 0.3)
+    sys.add_species(M.Homopolymer(B, 100, 1.0), 0.3)
+    itx = M.FloryInteraction()
+    itx.set_interaction(A, B, 0.5)
+    itx.set_interaction(A, C, 1.25)
+    itx.set_interaction(B, C, 1.25)
+    sys.add_interaction(itx)
+    M.fieldinit(sys, _julia_seed_fields("nbblend"))
+    return sys

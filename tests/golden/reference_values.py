@@ -77,3 +77,18 @@ TEST_UPDATERS = {
     "after_nag_commented_out": 0.06172669754976512,
     "after_anderson": 0.12798422498635653,
 }
+
+# examples/examples.ipynb cells 11-12: the ABC blend of BLEND_FINAL on 256x1x1 (L 20) from
+# fieldinit!(sys; scale = 0.05, seed = 12345), relaxed by scft!(sys, MomentumUpdater(method =
+# :MOM, lam = 0.01); opts = SCFTOptions(nsteps = 5000, nsout = 500, ftol = 1e-5, stol = 5e-5)).
+# Printed lines "Step (k / 5000): ferr = %8e, fhelm = %.5e" (the state after k updates) and
+# "Converged @ step = 3272: ferr = %8e, fhelm = %.5e" (the state after 3273 updates: the
+# loop breaks before incrementing its counter); the SCFTResults it returned are BLEND_FINAL.
+NOTEBOOK_BLEND_RUN = {
+    "printed": {0: (1.409117e+00, -7.42676e-02), 500: (5.151726e-02, -4.78117e-02),
+                1000: (4.316219e-03, -4.73547e-02), 1500: (9.502502e-04, -4.72453e-02),
+                2000: (2.516323e-04, -4.72159e-02), 2500: (6.925002e-05, -4.72081e-02),
+                3000: (1.963959e-05, -4.72061e-02)},
+    "converged_line": (9.986285e-06, -4.72057e-02),
+    "nsteps": 3272,
+}

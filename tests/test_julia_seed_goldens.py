@@ -84,3 +84,26 @@ def test_oracle_reproduces_test_updaters_goldens():
         u3.step()
     assert sys.free_energy() == pytest.approx(g["after_anderson"], rel=1e-9)
     assert sys.free_energy() == pytest.approx(g["after_anderson"], rel=math.sqrt(np.finfo(float).eps))
+
+
+def test_oracle_replays_the_notebooks_seeded_momentum_run():
+    """examples/examples.ipynb cells 11-12 from the seed: every line scft! printed (the state
+    after k updates, formatted as the reference formats it), the convergence step and the
+    returned SCFTResults.  About 20 s: 3273 MomentumUpdater steps of the 256-point blend."""
+    run = RV.NOTEBOOK_BLEND_RUN
+    sys = W.notebook_blend_seeded_system(O)
+    sys.residuals_update()  # scft! starts with residuals!(sys) (simulate.jl:66)
+    state = {0: (sys.field_error(), sys.free_energy())}
+    r = O.scft(sys, O.MomentumUpdater(method="MOM", lam=0.01),
+               opts=O.SCFTOptions(nsteps=5000, nsout=0, ftol=1e-5, stol=5e-5))
+    for step, ferr, fhelm in r.history:
+        state[step + 1] = (ferr, fhelm)
+    for k, (ferr, fhelm) in run["printed"].items():
+        assert f"{state[k][0]:8e}" == f"{ferr:8e}", k
+        assert f"{state[k][1]:.5e}" == f"{fhelm:.5e}", k
+    ferr, fhelm = run["converged_line"]  # "Converged @ step = n": the state after n + 1 updates
+    assert f"{state[run['nsteps'] + 1][0]:8e}" == f"{ferr:8e}"
+    assert f"{state[run['nsteps'] + 1][1]:.5e}" == f"{fhelm:.5e}"
+    assert r.converged and r.nsteps == run["nsteps"]
+    assert r.ferr == pytest.approx(RV.BLEND_FINAL["ferr"], rel=1e-9)
+    assert r.fhelm == pytest.approx(RV.BLEND_FINAL["fhelm"], rel=1e-13)
