@@ -19,8 +19,10 @@ reference tree, so each piece is restated here from its published algorithm:
    is the sign, bits 1..8 the layer, bits 1..51 the abscissa.  The layer tables use the right
    edge r = 3.6541528853610088 and a layer area v that is computed exactly from r (below,
    in 50-digit arithmetic).  For a `Float64` array of 13 or more elements, `randn!` first
-   takes one raw draw per element from the cache, then converts them in order.  Any
-   rejection draws a conversion needs come after the whole block.
+   takes one raw draw per element, then converts them in order.  Any rejection draws a
+   conversion needs come after the whole block.  The raw draws come from the cache for
+   arrays of up to 383 elements.  Longer arrays are generated straight from the state (see
+   `MersenneTwister.raw_array`); that path follows the same runtime but no golden pins it.
 3. `Dict` iteration order: slots in ascending order, a key's home slot is
    `hash(key) & (sz - 1)` in a table of 16 slots, with linear probing; `hash(::Int64)` is
    Thomas Wang's 64-bit integer mix of `3|x| + bits(Float64(x))`.  For monomer ids (1, 2, 3)
@@ -138,10 +140,11 @@ class MersenneTwister:
         self._cache: List[int] = []
         self._next = _CACHE
 
-    def _refill(self):
-        """Block generation of _CACHE / 2 words: the first _NW words come from the state, later
-        ones from the block itself; the state becomes the block's last _NW words."""
-        st, m = self._state, _CACHE // 2
+    def _block(self, m: int) -> List[int]:
+        """Block generation of m >= _NW words (2 m doubles as raw bits): the first _NW words
+        come from the state, later ones from the block itself; the state becomes the block's
+        last _NW words."""
+        st = self._state
         lung = st[_NW]
         out: List[Tuple[int, int]] = []
         for i in range(m):
@@ -151,8 +154,22 @@ class MersenneTwister:
             word, lung = _step(a, b, lung)
             out.append(word)
         self._state = out[m - _NW:] + [lung]
-        self._cache = [x for word in out for x in word]
+        return [x for word in out for x in word]
+
+    def _refill(self):
+        self._cache = self._block(_CACHE // 2)
         self._next = 0
+
+    def raw_array(self, n: int) -> List[int]:
+        """`rand!(rng, A, CloseOpen12())` for a Float64 array of n elements.  Up to n2 =
+        2 floor((n - 2) / 2) < 382: n draws from the cache.  Larger: n2 values by one block
+        generation straight from the state (the cache is left as it is), then n - n2 from
+        the cache.  (The first path is the one the reference's goldens pin; no golden here
+        covers the second.)"""
+        n2 = (n - 2) // 2 * 2
+        if n2 < 2 * _NW:
+            return [self.raw() for _ in range(n)]
+        return self._block(n2 // 2) + [self.raw() for _ in range(n - n2)]
 
     def raw(self) -> int:
         """IEEE bits of the next double in [1, 2)."""
@@ -238,7 +255,7 @@ def randn_array(rng: MersenneTwister, n: int) -> List[float]:
     """`randn!(rng, A)` for a Float64 array of n elements, in linear (column-major) order."""
     if n < 13:
         return [randn(rng) for _ in range(n)]
-    block = [rng.raw() for _ in range(n)]
+    block = rng.raw_array(n)
     return [_normal_from_bits(rng, b) for b in block]
 
 
