@@ -546,7 +546,9 @@ def scfstress(sys: FieldSystem) -> np.ndarray:
 # =============================================================================
 class AndersonUpdater:
     """AndersonUpdater(; nhist = 50, iter_euler = 1, lam_euler = 0.01) — anderson.jl:36-47.
-    The history lives on the device of the system it is set up with."""
+    The history lives on the device of the system it is set up with.  The engine keeps one
+    Anderson history per system: once a second AndersonUpdater is set up on a system, the
+    first one raises RuntimeError instead of stepping with the second one's history."""
 
     def __init__(self, nhist: int = 50, iter_euler: int = 1, lam_euler: float = 0.01):
         self.nhist = int(nhist)
@@ -554,12 +556,19 @@ class AndersonUpdater:
         self.lam_euler = float(lam_euler)
         self.system: Optional[FieldSystem] = None
 
+    def _owns(self, sys: FieldSystem) -> None:
+        if getattr(sys, "_anderson", None) is not self:
+            raise RuntimeError("another AndersonUpdater was set up on this system since; the GPU engine keeps "
+                               "one Anderson history per system")
+
     def _bind(self, sys: FieldSystem) -> None:
         """Create the updater's history on sys (once per system) and make it the current one."""
         if self.system is not sys:
             L.check(L.load().pf_anderson_create(sys._h, self.nhist, self.iter_euler, self.lam_euler), sys._h)
             self.system = sys
+            sys._anderson = self
         else:
+            self._owns(sys)
             L.check(L.load().pf_updater_select(sys._h, -1), sys._h)
 
     def setup(self, sys: FieldSystem) -> None:
@@ -571,6 +580,7 @@ class AndersonUpdater:
         """step!(updater) — anderson.jl:98-228."""
         if self.system is None:
             raise RuntimeError("AndersonUpdater is not set up")
+        self._owns(self.system)
         L.check(L.load().pf_anderson_step(self.system._h), self.system._h)
 
 

@@ -78,3 +78,19 @@ def test_no_gpu_fails_loudly(lib_path):
         pass
     with pytest.raises(pf.PolyFieldsError):
         pf.FieldSystem((64, 1, 1), pf.UnitCell(1, "lamellar", 10.0))
+
+
+def test_superseded_anderson_updater_fails_loudly():
+    """The engine keeps one Anderson history per system: an AndersonUpdater whose system has
+    since had another one set up raises instead of stepping with the other's history."""
+    import types
+
+    import polyfields as pf
+    u1, u2 = pf.AndersonUpdater(nhist=5), pf.AndersonUpdater(nhist=5)
+    sys_ = types.SimpleNamespace(_anderson=u2)
+    u2._owns(sys_)
+    with pytest.raises(RuntimeError, match="one Anderson history per system"):
+        u1._owns(sys_)
+    u1.system = sys_
+    with pytest.raises(RuntimeError, match="one Anderson history per system"):
+        u1.step()
