@@ -5,6 +5,7 @@ src/system/system.jl, src/interactions/flory.jl, src/system/compress.jl,
 src/updaters/anderson.jl); the C++ one, with its own mixed-radix FFT, is bench.py's timed CPU
 baseline.  Propagators, densities, residuals, free energy and field error agree to 1e-12
 relative; ten Anderson steps (whose small least-squares solve amplifies rounding) to 1e-9.
+The restatement also reproduces the reference's own test/test_system.jl goldens.
 """
 import numpy as np
 import pytest
@@ -76,3 +77,17 @@ def test_iteration_matches_oracle(name, make):
 def test_uses_several_threads():
     c = C.CpuSystem((16, 1, 1), np.zeros((1, 1, 9)))
     assert c.threads >= 1
+
+
+def test_reproduces_the_reference_test_system_goldens():
+    """test/test_system.jl:29-33 on the C++ restatement itself (the timed reference arm): the
+    seeded fields of fieldinit! (Julia's randn stream, fixture julia_seed_fields.npz), then
+    density! of each species and free_energy."""
+    import reference_values as RV
+    o, _, _ = W.reference_test_system(O)
+    c = C.CpuSystem.from_oracle(o)
+    c.residuals()  # density! at the fields fieldinit! left (mean-subtracted)
+    g = RV.TEST_SYSTEM
+    assert c.species_q(0) == pytest.approx(g["point_Q"], rel=1e-13)
+    assert c.species_q(1) == pytest.approx(g["chain_Q"], rel=1e-13)
+    assert c.free_energy() == pytest.approx(g["free_energy"], rel=1e-13)
