@@ -481,7 +481,9 @@ def run_sweep(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 40 SCFT iterations on the GPU, about 0.4 s, so that the "
+                         "100 ms clock sampler sees several samples; 10 for --impl reference)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=N_GRID, help="grid points per axis (default 128)")
@@ -501,6 +503,8 @@ def main():
                     help="sweep: float64 phase of the mixed runs (SCFTOptions.polish)")
     ap.add_argument("--switch", type=float, default=1e-5, help="sweep: ferr at which the mixed runs switch to float64")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 10 if args.impl == "reference" else 40
     if args.impl == "reference":
         return run_reference(args)
     if args.mode == "profile":
