@@ -19,6 +19,7 @@ from typing import Dict, List, Optional, Sequence
 import numpy as np
 
 from . import _lib as L
+from . import julia_random
 
 Canonical = "Canonical"
 Grand = "Grand"
@@ -889,8 +890,10 @@ def fieldinit(sys: FieldSystem, fields=None, *, field_type: str = "omega", inter
               load_cell: bool = True, seed: int = -1, scale: float = 0.1) -> None:
     """fieldinit!(sys, fields::Dict; field_type, interpolate) (fileio.jl:25-54),
     fieldinit!(sys, path; load_cell, interpolate) (fileio.jl:56-64) when ``fields`` is a path to
-    a savefields JSON, or, without ``fields``, fieldinit!(sys; seed, scale) (fileio.jl:14-23)
-    with NumPy's PCG64 normal stream in place of Julia's MersenneTwister randn.
+    a savefields JSON, or, without ``fields``, fieldinit!(sys; seed, scale) (fileio.jl:14-23):
+    the reference's seeded stream (Julia's MersenneTwister randn in its Dict order of the
+    monomer ids, polyfields.julia_random), so a seed gives the reference's fields; seed < 0
+    continues the process-wide stream.
 
     Grids of another shape are resampled with interpolate_grid (or rejected with
     interpolate=False).  field_type "rho" takes densities: the fields become their potentials,
@@ -902,8 +905,7 @@ def fieldinit(sys: FieldSystem, fields=None, *, field_type: str = "omega", inter
         fieldinit(sys, data["fields"], field_type=data["field_type"], interpolate=interpolate)
         return
     if fields is None:
-        rng = np.random.Generator(np.random.PCG64(seed if seed >= 0 else None))
-        fields = {mid: scale * rng.standard_normal(sys.shape) for mid in sorted(sys.monomers)}
+        fields = julia_random.fieldinit_fields(list(sys.monomers), sys.shape, seed, scale)
     ftype = str(field_type).lstrip(":")
     if ftype not in ("omega", "rho"):
         raise ValueError(f"unknown field_type {field_type}")

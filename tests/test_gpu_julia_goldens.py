@@ -75,3 +75,27 @@ def test_test_updaters_goldens_fp64():
     ug[0].step()
     uo[0].step()
     assert s.free_energy() == pytest.approx(o.free_energy(), rel=1e-8)
+
+
+def test_seeded_fieldinit_as_the_reference_test_writes_it():
+    """test/test_system.jl:3-33 line for line through the Python mirror: its own seeded
+    fieldinit (Julia's stream, polyfields.julia_random) instead of the fixture."""
+    amon = pf.Monomer(1, 1.0, 0.0)
+    bmon = pf.Monomer(2, 1.0, 0.0)
+    cmon = pf.Monomer(3, 1.0, 0.0)
+    point = pf.Point(cmon)
+    chain = pf.Diblock(amon, bmon, 100, 0.5, 1.0, 1.0, 100)
+    itx = pf.FloryInteraction()
+    itx.set_interaction(amon, bmon, 0.2)
+    sys = pf.FieldSystem((32, 1, 1), pf.UnitCell(1, "lamellar", 10.0), monomers=[amon, bmon, cmon],
+                         precision="fp64")
+    sys.add_species(point, 0.75)
+    sys.add_species(chain, 0.25)
+    sys.add_interaction(itx)
+    pf.fieldinit(sys, scale=0.1, seed=12345)
+    sys.density_update()
+    g = RV.TEST_SYSTEM
+    assert point.Q == pytest.approx(g["point_Q"], rel=FP64_RTOL)
+    assert chain.Q == pytest.approx(g["chain_Q"], rel=FP64_RTOL)
+    assert sys.free_energy() == pytest.approx(g["free_energy"], rel=FP64_RTOL)
+    assert sys.scfstress()[0] == pytest.approx(g["scfstress_1"], rel=1e-9)

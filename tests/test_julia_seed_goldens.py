@@ -107,3 +107,39 @@ def test_oracle_replays_the_notebooks_seeded_momentum_run():
     assert r.converged and r.nsteps == run["nsteps"]
     assert r.ferr == pytest.approx(RV.BLEND_FINAL["ferr"], rel=1e-9)
     assert r.fhelm == pytest.approx(RV.BLEND_FINAL["fhelm"], rel=1e-13)
+
+
+# ----------------------------------------------------------------------------- the package's stream
+def test_package_fieldinit_stream_gives_the_fixture():
+    """polyfields.julia_random (what pf.fieldinit(sys; seed, scale) draws) writes exactly the
+    fields of the fixture, i.e. the reference's fieldinit! fields for its tests and notebook."""
+    from polyfields import julia_random as JR
+    d = np.load(f"{W.GOLDEN}/julia_seed_fields.npz")
+    for name, mids, shape, scale in (("system", (1, 2, 3), (1, 1, 32), 0.1), ("updaters", (1, 2), (1, 1, 32), 0.1),
+                                     ("nbblend", (1, 2, 3), (1, 1, 256), 0.05)):
+        got = JR.fieldinit_fields(mids, shape, seed=12345, scale=scale)
+        assert sorted(got) == sorted(mids)
+        for mid in mids:
+            assert np.array_equal(got[mid], d[f"{name}_w{mid}"]), (name, mid)
+
+
+@pytest.mark.parametrize("seed", [12345, 1234, 0, 2 ** 40 + 7])
+def test_package_stream_matches_the_oracle_restatement(seed):
+    """The package's vectorised generator against the oracle's word-by-word one, bit for bit:
+    scalar draws, the cache path (< 384 elements), the direct block fill (>= 384) and the
+    ziggurat's rejection draws."""
+    pytest.importorskip("mpmath")
+    from polyfields import julia_random as JR
+    a, b = J.MersenneTwister(seed), JR.MersenneTwister(seed)
+    for n in (5, 13, 32, 256, 383, 384, 385, 1003, 5000, 7):
+        assert np.array_equal(np.array(J.randn_array(a, n)), b.randn_array(n)), n
+    assert a.rand() == b.rand()
+
+
+def test_package_ziggurat_tables_are_the_oracles():
+    pytest.importorskip("mpmath")
+    from polyfields import julia_random as JR
+    k, w, f = JR._zig()
+    ko, wo, fo = J._tables()
+    assert [int(x) for x in k] == list(ko)
+    assert np.array_equal(w, np.array(wo)) and np.array_equal(f, np.array(fo))
