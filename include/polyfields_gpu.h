@@ -56,7 +56,12 @@ typedef struct pf_system pf_system;
  * restarted GMRES over float32 finite-difference Jacobian products; runs without a
  * DomainUpdater; falls back to the field updater's float64 steps if a Newton step stalls),
  * 1 = float64 steps of the field updater (the Anderson history restarted at the switch),
- * 0 = automatic: Newton-Krylov on 3D grids, field-updater steps on 1D and 2D grids. */
+ * 0 = automatic: Newton-Krylov on 3D grids, field-updater steps on 1D and 2D grids.
+ * Output: with nsout > 0 scft prints the reference's lines (simulate.jl:82-117: the header,
+ * "Step (k / n)" every nsout steps, "Updating cell dimensions", "Converged @ step").  With
+ * nsout = 0 it prints nothing; the reference still prints its header and the cell and
+ * convergence lines there.  A library call stays quiet by default, and batched runs do not
+ * interleave their output. */
 typedef struct pf_scft_options {
   int nsteps;
   int nsout;
