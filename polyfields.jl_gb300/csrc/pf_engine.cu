@@ -2206,7 +2206,14 @@ struct System {
       if (std::isnan(ferr)) throw PFError(E_NAN, "Diverging field updater -- breaking.");
       converged = isconverged(ferr, o.ftol, serr, o.stol, vcell);
       if (converged) {
-        if (o.nsout > 0) printf("Converged @ step = %d: ferr = %8e, fhelm = %.5e\n", step, ferr, fhelm);
+        if (o.nsout > 0) {
+          printf("Converged @ step = %d: ferr = %8e, fhelm = %.5e\n", step, ferr, fhelm);
+          if (vcell) {  // simulate.jl:115-117
+            printf("Converged cell parameters: [");
+            for (int i = 0; i < cell.np(); ++i) printf("%s%.17g", i ? ", " : "", cell.params[i]);
+            printf("]\n");
+          }
+        }
         break;
       }
       if (o.nsave > 0 && step % o.nsave == 0 && !savepath.empty()) save_fields(savepath);  // simulate.jl:124-128
