@@ -143,3 +143,15 @@ def test_package_ziggurat_tables_are_the_oracles():
     ko, wo, fo = J._tables()
     assert [int(x) for x in k] == list(ko)
     assert np.array_equal(w, np.array(wo)) and np.array_equal(f, np.array(fo))
+
+
+def test_negative_seed_continues_the_stream():
+    """fieldinit!(sys; seed = -1) does not reseed (src/fileio.jl:15-17): a second call continues
+    the process-wide stream."""
+    from polyfields import julia_random as JR
+    first = JR.fieldinit_fields((1, 2), (1, 4, 8), seed=7, scale=1.0)
+    second = JR.fieldinit_fields((1, 2), (1, 4, 8), seed=-1, scale=1.0)
+    rng = JR.MersenneTwister(7)
+    expect = [rng.randn_array(32) for _ in range(4)]   # Dict order (2, 1), then again
+    assert np.array_equal(first[2].ravel(), expect[0]) and np.array_equal(first[1].ravel(), expect[1])
+    assert np.array_equal(second[2].ravel(), expect[2]) and np.array_equal(second[1].ravel(), expect[3])
