@@ -179,6 +179,7 @@ struct FFT3 {
   int nx, ny, nz, kx;
   Plan1D px, py, pz;
   static constexpr long kChunk = 64;  // complex values per z-transform chunk
+  static constexpr int kPairs = 8;    // row pairs per batched x transform
   FFT3(int x, int y, int z) : nx(x), ny(y), nz(z), kx(x / 2 + 1), px(x), py(y), pz(z) {}
 
   void zpass(cplx* k, int sign) const {
@@ -198,62 +199,121 @@ struct FFT3 {
     }
   }
 
-  // real r[z][y][x] -> half spectrum k[z][y][kx] (unnormalised)
-  void forward(const double* r, cplx* k) const {
+  // forward z transform, multiply by ld, inverse z transform, chunk by chunk (the spectrum
+  // between the two transforms never leaves the chunk buffer)
+  void zfilter(cplx* k, const double* ld) const {
+    const long plane = (long)ny * kx;
+    const long nchunk = (plane + kChunk - 1) / kChunk;
 #pragma omp parallel
     {
-      std::vector<C2> a(std::max((long)nx, (long)ny * kx)), b(a.size());
+      std::vector<C2> a((size_t)nz * kChunk), b(a.size());
+#pragma omp for schedule(static)
+      for (long c = 0; c < nchunk; ++c) {
+        const long c0 = c * kChunk, B = std::min(kChunk, plane - c0);
+        C2* src = reinterpret_cast<C2*>(k);
+        for (int z = 0; z < nz; ++z) std::memcpy(&a[(size_t)z * B], src + (long)z * plane + c0, sizeof(C2) * B);
+        fft_batch(pz, a.data(), b.data(), B, -1);
+        for (int z = 0; z < nz; ++z) {
+          const double* l = ld + (long)z * plane + c0;
+          C2* v = &a[(size_t)z * B];
+          for (long j = 0; j < B; ++j) v[j] = C2{v[j].r * l[j], v[j].i * l[j]};
+        }
+        fft_batch(pz, a.data(), b.data(), B, +1);
+        for (int z = 0; z < nz; ++z) std::memcpy(src + (long)z * plane + c0, &a[(size_t)z * B], sizeof(C2) * B);
+      }
+    }
+  }
+
+  // real r[z][y][x] -> half spectrum k[z][y][kx] (unnormalised); with lw, transforms lw * r
+  // (one multiply per point, as the load into the x transform), and leaves out the z pass
+  // (xy_only, for zfilter)
+  void forward(const double* r, cplx* k, const double* lw = nullptr, bool xy_only = false) const {
+#pragma omp parallel
+    {
+      std::vector<C2> a(std::max((long)nx * kPairs, (long)ny * kx)), b(a.size());
 #pragma omp for schedule(static)
       for (int z = 0; z < nz; ++z) {
         C2* kp = reinterpret_cast<C2*>(k) + (long)z * ny * kx;
-        for (int y = 0; y < ny; y += 2) {  // rows y, y+1 as the real and imaginary parts
-          const double* r0 = r + ((long)z * ny + y) * nx;
-          const double* r1 = (y + 1 < ny) ? r0 + nx : nullptr;
-          for (int x = 0; x < nx; ++x) a[x] = C2{r0[x], r1 ? r1[x] : 0.0};
-          fft_batch(px, a.data(), b.data(), 1, -1);
-          C2* k0 = kp + (long)y * kx;
-          for (int i = 0; i < kx; ++i) {
-            const C2 zk = a[i], zn = a[(nx - i) % nx];
-            k0[i] = C2{0.5 * (zk.r + zn.r), 0.5 * (zk.i - zn.i)};
-            if (r1) k0[kx + i] = C2{0.5 * (zk.i + zn.i), 0.5 * (zn.r - zk.r)};
+        // rows y, y+1 as the real and imaginary parts of one complex row; P such row pairs
+        // side by side (element x of pair p at a[x P + p]) in one batched transform
+        for (int y0 = 0; y0 < ny; y0 += 2 * kPairs) {
+          const int P = std::min(kPairs, (ny - y0 + 1) / 2);
+          for (int p = 0; p < P; ++p) {
+            const int y = y0 + 2 * p;
+            const double* r0 = r + ((long)z * ny + y) * nx;
+            const double* r1 = (y + 1 < ny) ? r0 + nx : nullptr;
+            if (lw) {
+              const double* l0 = lw + ((long)z * ny + y) * nx;
+              for (int x = 0; x < nx; ++x) a[(long)x * P + p] = C2{l0[x] * r0[x], r1 ? l0[nx + x] * r1[x] : 0.0};
+            } else {
+              for (int x = 0; x < nx; ++x) a[(long)x * P + p] = C2{r0[x], r1 ? r1[x] : 0.0};
+            }
+          }
+          fft_batch(px, a.data(), b.data(), P, -1);
+          for (int p = 0; p < P; ++p) {
+            const int y = y0 + 2 * p;
+            const bool two = y + 1 < ny;
+            C2* k0 = kp + (long)y * kx;
+            for (int i = 0; i < kx; ++i) {
+              const C2 zk = a[(long)i * P + p], zn = a[(long)((nx - i) % nx) * P + p];
+              k0[i] = C2{0.5 * (zk.r + zn.r), 0.5 * (zk.i - zn.i)};
+              if (two) k0[kx + i] = C2{0.5 * (zk.i + zn.i), 0.5 * (zn.r - zk.r)};
+            }
           }
         }
         if (ny > 1) fft_batch(py, kp, b.data(), kx, -1);
       }
     }
-    if (nz > 1) zpass(k, -1);
+    if (nz > 1 && !xy_only) zpass(k, -1);
   }
 
-  // half spectrum k (overwritten) -> real r, unnormalised inverse (the caller folds 1/Ng in)
-  void inverse(cplx* k, double* r) const {
-    if (nz > 1) zpass(k, +1);
+  // half spectrum k (overwritten) -> real r, unnormalised inverse (the caller folds 1/Ng in);
+  // with lw, writes lw * r; xy_only leaves out the z pass (done by zfilter)
+  void inverse(cplx* k, double* r, const double* lw = nullptr, bool xy_only = false) const {
+    if (nz > 1 && !xy_only) zpass(k, +1);
 #pragma omp parallel
     {
-      std::vector<C2> a(std::max((long)nx, (long)ny * kx)), b(a.size());
+      std::vector<C2> a(std::max((long)nx * kPairs, (long)ny * kx)), b(a.size());
 #pragma omp for schedule(static)
       for (int z = 0; z < nz; ++z) {
         C2* kp = reinterpret_cast<C2*>(k) + (long)z * ny * kx;
         if (ny > 1) fft_batch(py, kp, b.data(), kx, +1);
-        for (int y = 0; y < ny; y += 2) {  // Hermitian halves of rows y, y+1 -> one complex transform
-          const bool two = y + 1 < ny;
-          const C2* k0 = kp + (long)y * kx;
-          const C2* k1 = two ? k0 + kx : nullptr;
-          for (int x = 0; x < nx; ++x) {
-            C2 A, Bv = {0.0, 0.0};
-            if (x < kx) {
-              A = k0[x];
-              if (two) Bv = k1[x];
-            } else {
-              A = C2{k0[nx - x].r, -k0[nx - x].i};
-              if (two) Bv = C2{k1[nx - x].r, -k1[nx - x].i};
+        // Hermitian halves of rows y, y+1 -> one complex row; P row pairs per batched transform
+        for (int y0 = 0; y0 < ny; y0 += 2 * kPairs) {
+          const int P = std::min(kPairs, (ny - y0 + 1) / 2);
+          for (int p = 0; p < P; ++p) {
+            const int y = y0 + 2 * p;
+            const bool two = y + 1 < ny;
+            const C2* k0 = kp + (long)y * kx;
+            const C2* k1 = two ? k0 + kx : nullptr;
+            for (int x = 0; x < nx; ++x) {
+              C2 A, Bv = {0.0, 0.0};
+              if (x < kx) {
+                A = k0[x];
+                if (two) Bv = k1[x];
+              } else {
+                A = C2{k0[nx - x].r, -k0[nx - x].i};
+                if (two) Bv = C2{k1[nx - x].r, -k1[nx - x].i};
+              }
+              a[(long)x * P + p] = C2{A.r - Bv.i, A.i + Bv.r};  // A + i B
             }
-            a[x] = C2{A.r - Bv.i, A.i + Bv.r};  // A + i B
           }
-          fft_batch(px, a.data(), b.data(), 1, +1);
-          double* r0 = r + ((long)z * ny + y) * nx;
-          for (int x = 0; x < nx; ++x) r0[x] = a[x].r;
-          if (two)
-            for (int x = 0; x < nx; ++x) r0[nx + x] = a[x].i;
+          fft_batch(px, a.data(), b.data(), P, +1);
+          for (int p = 0; p < P; ++p) {
+            const int y = y0 + 2 * p;
+            const bool two = y + 1 < ny;
+            double* r0 = r + ((long)z * ny + y) * nx;
+            if (lw) {
+              const double* l0 = lw + ((long)z * ny + y) * nx;
+              for (int x = 0; x < nx; ++x) r0[x] = l0[x] * a[(long)x * P + p].r;
+              if (two)
+                for (int x = 0; x < nx; ++x) r0[nx + x] = l0[nx + x] * a[(long)x * P + p].i;
+            } else {
+              for (int x = 0; x < nx; ++x) r0[x] = a[(long)x * P + p].r;
+              if (two)
+                for (int x = 0; x < nx; ++x) r0[nx + x] = a[(long)x * P + p].i;
+            }
+          }
         }
       }
     }
@@ -310,32 +370,34 @@ struct System {
     for (long i = 0; i < nk; ++i) ld[i] = std::exp(-cd * ksq[i]) * inv;
   }
   // propagate! :RK2 (mde.jl:76-81): qout = LW1 * irfft(LD1 * rfft(LW1 * qin))
+  // The LW multiplies ride the x transforms' loads and stores; on 3D grids the LD multiply
+  // sits between the forward and inverse z transforms of each chunk (FFT3::zfilter).
   void propagate(const double* qin, double* qout) {
+    fft.forward(qin, qk.data(), lw.data(), true);
+    if (nz > 1) {
+      fft.zfilter(qk.data(), ld.data());
+    } else {
 #pragma omp parallel for schedule(static)
-    for (long i = 0; i < ng; ++i) qr[i] = lw[i] * qin[i];
-    fft.forward(qr.data(), qk.data());
-#pragma omp parallel for schedule(static)
-    for (long i = 0; i < nk; ++i) qk[i] = cplx(qk[i].real() * ld[i], qk[i].imag() * ld[i]);
-    fft.inverse(qk.data(), qr.data());
-#pragma omp parallel for schedule(static)
-    for (long i = 0; i < ng; ++i) qout[i] = lw[i] * qr[i];
+      for (long i = 0; i < nk; ++i) qk[i] = cplx(qk[i].real() * ld[i], qk[i].imag() * ld[i]);
+    }
+    fft.inverse(qk.data(), qout, lw.data(), true);
   }
 
   // density!(::Multiblock) (multiblock.jl:125-231); block densities added to rho with phi / (Q Nref)
   void chain_density(Species& sp) {
     const int nb = (int)sp.mon.size(), Ns = sp.Ns;
     sp.q.resize((size_t)(Ns + 1) * ng);
-    sp.qc.resize((size_t)(Ns + 1) * ng);
     double* q = sp.q.data();
-    double* qc = sp.qc.data();
     std::fill(q, q + ng, 1.0);
     for (int ib = 0; ib < nb; ++ib) {
       update(w[sp.mon[ib]], vol[sp.mon[ib]], sp.b[ib], sp.ds[ib]);
       for (int s = sp.begin[ib]; s < sp.begin[ib + 1]; ++s) propagate(q + (long)(s - 1) * ng, q + (long)s * ng);
     }
-    if (nb == 1) {
-      for (int s = 0; s <= Ns; ++s) std::memcpy(qc + (long)s * ng, q + (long)(Ns - s) * ng, sizeof(double) * ng);
-    } else {
+    // one block: qc_s = q_{Ns - s} (the chain reads the same from both ends), used in place
+    double* qc = nullptr;
+    if (nb > 1) {
+      sp.qc.resize((size_t)(Ns + 1) * ng);
+      qc = sp.qc.data();
       std::fill(qc + (long)Ns * ng, qc + (long)(Ns + 1) * ng, 1.0);
       for (int ib = nb - 1; ib >= 0; --ib) {
         update(w[sp.mon[ib]], vol[sp.mon[ib]], sp.b[ib], sp.ds[ib]);
@@ -348,18 +410,40 @@ struct System {
     for (long i = 0; i < ng; ++i) qsum += q[(long)Ns * ng + i];
     sp.Q = qsum / (double)ng;
     const double scale = sp.phi / (sp.Q * sp.Nref);  // muphi! canonical: phi_sp rho_sp
+    auto qplane = [&](int s) { return q + (long)s * ng; };
+    auto qcplane = [&](int s) { return qc ? qc + (long)s * ng : q + (long)(Ns - s) * ng; };
+    // Simpson over the block's contour points, a chunk of grid points at a time: each chunk
+    // streams the planes in order (per point the sums run in ascending s, as a point-by-point
+    // loop would)
+    constexpr long kCh = 2048;
     for (int ib = 0; ib < nb; ++ib) {
       const int bgn = sp.begin[ib], end = sp.begin[ib + 1];
       const double f = sp.ds[ib] / 3.0;
       double* out = rho[sp.mon[ib]].data();
-#pragma omp parallel for schedule(static)
-      for (long i = 0; i < ng; ++i) {
-        double r = q[(long)(bgn - 1) * ng + i] * qc[(long)(bgn - 1) * ng + i];
-        r += q[(long)(end - 1) * ng + i] * qc[(long)(end - 1) * ng + i];
-        double r4 = 0.0, r2 = 0.0;
-        for (int s = bgn + 1; s < end; s += 2) r4 += q[(long)(s - 1) * ng + i] * qc[(long)(s - 1) * ng + i];
-        for (int s = bgn + 2; s < end - 1; s += 2) r2 += q[(long)(s - 1) * ng + i] * qc[(long)(s - 1) * ng + i];
-        out[i] += (r + 4.0 * r4 + 2.0 * r2) * f * scale;
+#pragma omp parallel
+      {
+        std::vector<double> r(kCh), r4(kCh), r2(kCh);
+#pragma omp for schedule(static)
+        for (long c0 = 0; c0 < ng; c0 += kCh) {
+          const long m = std::min(kCh, ng - c0);
+          const double *qa = qplane(bgn - 1) + c0, *ca = qcplane(bgn - 1) + c0;
+          const double *qb = qplane(end - 1) + c0, *cb = qcplane(end - 1) + c0;
+          for (long i = 0; i < m; ++i) {
+            r[i] = qa[i] * ca[i];
+            r[i] += qb[i] * cb[i];
+            r4[i] = 0.0;
+            r2[i] = 0.0;
+          }
+          for (int s = bgn + 1; s < end; s += 2) {
+            const double *qs = qplane(s - 1) + c0, *cs = qcplane(s - 1) + c0;
+            for (long i = 0; i < m; ++i) r4[i] += qs[i] * cs[i];
+          }
+          for (int s = bgn + 2; s < end - 1; s += 2) {
+            const double *qs = qplane(s - 1) + c0, *cs = qcplane(s - 1) + c0;
+            for (long i = 0; i < m; ++i) r2[i] += qs[i] * cs[i];
+          }
+          for (long i = 0; i < m; ++i) out[c0 + i] += (r[i] + 4.0 * r4[i] + 2.0 * r2[i]) * f * scale;
+        }
       }
     }
   }
