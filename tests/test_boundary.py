@@ -94,3 +94,44 @@ def test_superseded_anderson_updater_fails_loudly():
     u1.system = sys_
     with pytest.raises(RuntimeError, match="one Anderson history per system"):
         u1.step()
+
+
+def _declared_params():
+    """{name: [parameter declarations]} of the header's entry points."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for name, params in re.findall(r"\b(pf_[a-z_0-9]+)\s*\(([^()]*)\)\s*;", text):
+        params = params.strip()
+        out[name] = [] if params in ("", "void") else [p.strip() for p in params.split(",")]
+    return out
+
+
+def test_julia_shim_calls_match_the_header():
+    """polyfields.jl_gb300/julia/PolyFieldsGPU.jl cannot run without Julia, so its ccalls are
+    checked against the header statically: every symbol is declared, with as many arguments,
+    pointers where the C side takes pointers and scalars where it takes scalars."""
+    shim = open(os.path.join(ROOT, "polyfields.jl_gb300", "julia", "PolyFieldsGPU.jl")).read()
+    calls = re.findall(r"ccall\(\(:(pf_[a-z_0-9]+),\s*lib\),\s*[\w{}]+,\s*\(([^()]*)\)", shim, flags=re.S)
+    assert len(calls) >= 20
+    decl = _declared_params()
+    for name, types in calls:
+        assert name in decl, name
+        jt = [t.strip() for t in types.split(",") if t.strip()]
+        assert len(jt) == len(decl[name]), (name, jt, decl[name])
+        for j, c in zip(jt, decl[name]):
+            j_ptr = j.startswith(("Ptr", "Ref", "Cstring"))
+            assert j_ptr == ("*" in c), (name, j, c)
+
+
+def test_julia_shim_structs_match_the_header():
+    """The shim's PFOptions / PFResults mirror pf_scft_options / pf_scft_results field by field
+    (same names, order and C types), so `Ref{PFOptions}` passes the layout the library reads."""
+    shim = open(os.path.join(ROOT, "polyfields.jl_gb300", "julia", "PolyFieldsGPU.jl")).read()
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    ctype = {"Cint": "int", "Cdouble": "double"}
+    for jname, cname in (("PFOptions", "pf_scft_options"), ("PFResults", "pf_scft_results")):
+        body = re.search(r"struct " + jname + r"\b.*?\n(.*?)\nend", shim, flags=re.S).group(1)
+        jf = re.findall(r"^\s*(\w+)::(\w+)", body, flags=re.M)
+        cbody = re.search(r"typedef struct " + cname + r"\s*\{(.*?)\}", text, flags=re.S).group(1)
+        cf = re.findall(r"^\s*(int|double)\s+(\w+)\s*;", cbody, flags=re.M)
+        assert [(n, ctype[t]) for n, t in jf] == [(n, t) for t, n in cf], jname
