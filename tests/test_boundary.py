@@ -135,3 +135,24 @@ def test_julia_shim_structs_match_the_header():
         cbody = re.search(r"typedef struct " + cname + r"\s*\{(.*?)\}", text, flags=re.S).group(1)
         cf = re.findall(r"^\s*(int|double)\s+(\w+)\s*;", cbody, flags=re.M)
         assert [(n, ctype[t]) for n, t in jf] == [(n, t) for t, n in cf], jname
+
+
+def test_ctypes_signatures_match_the_header():
+    """polyfields/_lib.py binds every entry point with the header's argument count, pointers
+    where the C side takes pointers, and struct layouts equal to the C typedefs."""
+    import ctypes
+
+    from polyfields import _lib as L
+    decl = _declared_params()
+    assert sorted(L.SIGNATURES) == sorted(decl)
+    for name, (_, args) in L.SIGNATURES.items():
+        assert len(args) == len(decl[name]), (name, args, decl[name])
+        for a, c in zip(args, decl[name]):
+            is_ptr = a in (ctypes.c_void_p, ctypes.c_char_p) or hasattr(a, "_type_") and a.__name__.startswith("LP_")
+            assert is_ptr == ("*" in c), (name, a, c)
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    ctype = {ctypes.c_int: "int", ctypes.c_double: "double"}
+    for cls, cname in ((L.ScftOptions, "pf_scft_options"), (L.ScftResults, "pf_scft_results")):
+        cbody = re.search(r"typedef struct " + cname + r"\s*\{(.*?)\}", text, flags=re.S).group(1)
+        cf = re.findall(r"^\s*(int|double)\s+(\w+)\s*;", cbody, flags=re.M)
+        assert [(n, ctype[t]) for n, t in cls._fields_] == [(n, t) for t, n in cf], cname
