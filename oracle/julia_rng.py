@@ -276,16 +276,30 @@ def _hash_int(x: int) -> int:
 
 
 def dict_order(keys: Sequence[int]) -> List[int]:
-    """Iteration order of a Julia `Dict{Int, V}` filled with `keys` in this order (16 slots;
-    up to 10 keys, below the table's first resize)."""
-    if len(keys) > 10:
-        raise ValueError("only tables below their first resize (<= 10 keys) are modelled")
-    slots: List = [None] * 16
-    for key in keys:
-        i = _hash_int(key) & 15
-        while slots[i] is not None and slots[i] != key:
-            i = (i + 1) & 15
+    """Iteration order of a Julia `Dict{Int, V}` filled with `keys` in this order: 16 slots to
+    start, linear probing from the home slot, and once more than 2/3 of the slots are taken a
+    rehash into max(16, nextpow2(4 count)) slots that reinserts the keys in slot order.  (The
+    reference's systems have a handful of monomers; beyond 10 keys no golden pins this.)"""
+    def place(slots, key):
+        m = len(slots) - 1
+        i = _hash_int(key) & m
+        while slots[i] is not None:
+            i = (i + 1) & m
         slots[i] = key
+
+    slots: List = [None] * 16
+    count = 0
+    for key in keys:
+        if key in slots:
+            continue
+        place(slots, key)
+        count += 1
+        if 3 * count > 2 * len(slots):
+            grown: List = [None] * max(16, 1 << (4 * count - 1).bit_length())
+            for k in slots:
+                if k is not None:
+                    place(grown, k)
+            slots = grown
     return [s for s in slots if s is not None]
 
 

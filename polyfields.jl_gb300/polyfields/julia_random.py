@@ -248,19 +248,37 @@ def _wang64(a: int) -> int:
     return (a + (a << 31)) & m
 
 
+def _slot_hash(key: int) -> int:
+    fbits = struct.unpack("<Q", struct.pack("<d", float(key)))[0]
+    return _wang64((3 * abs(key) + fbits) & ((1 << 64) - 1))
+
+
 def dict_order(keys: Sequence[int]) -> List[int]:
-    """Iteration order of a Julia `Dict{Int}` holding `keys` (inserted in this order; up to 10
-    keys, the 16-slot table before its first resize)."""
-    if len(keys) > 10:
-        raise ValueError("Dict order is modelled for up to 10 keys")
-    slots: List[Optional[int]] = [None] * 16
-    for key in keys:
-        fbits = struct.unpack("<Q", struct.pack("<d", float(key)))[0]
-        i = _wang64((3 * abs(key) + fbits) & ((1 << 64) - 1)) & 15
-        while slots[i] is not None and slots[i] != key:
-            i = (i + 1) & 15
+    """Iteration order of a Julia `Dict{Int}` holding `keys` (inserted in this order): 16
+    slots, linear probing, and a rehash into max(16, nextpow2(4 count)) slots (keys reinserted
+    in slot order) once more than 2/3 of the slots are taken."""
+    table: List[Optional[int]] = [None] * 16
+
+    def place(slots: List[Optional[int]], key: int) -> None:
+        m = len(slots) - 1
+        i = _slot_hash(key) & m
+        while slots[i] is not None:
+            i = (i + 1) & m
         slots[i] = key
-    return [s for s in slots if s is not None]
+
+    count = 0
+    for key in keys:
+        if key in table:
+            continue
+        place(table, key)
+        count += 1
+        if 3 * count > 2 * len(table):
+            grown: List[Optional[int]] = [None] * max(16, 1 << (4 * count - 1).bit_length())
+            for k in table:
+                if k is not None:
+                    place(grown, k)
+            table = grown
+    return [k for k in table if k is not None]
 
 
 _global: Optional[MersenneTwister] = None

@@ -155,3 +155,15 @@ def test_negative_seed_continues_the_stream():
     expect = [rng.randn_array(32) for _ in range(4)]   # Dict order (2, 1), then again
     assert np.array_equal(first[2].ravel(), expect[0]) and np.array_equal(first[1].ravel(), expect[1])
     assert np.array_equal(second[2].ravel(), expect[2]) and np.array_equal(second[1].ravel(), expect[3])
+
+
+def test_dict_order_beyond_the_first_resize():
+    """Eleven or more monomer ids: the table grows (64 slots for 11 keys); the package and
+    the oracle model it alike, and the order of up to 10 keys is unchanged by the growth rule."""
+    from polyfields import julia_random as JR
+    rng = np.random.default_rng(3)
+    for n in (1, 3, 10, 11, 12, 25, 40):
+        keys = [int(k) for k in rng.choice(1000, size=n, replace=False)]
+        got = JR.dict_order(keys)
+        assert got == J.dict_order(keys) and sorted(got) == sorted(keys), n
+    assert JR.dict_order([1, 2, 3]) == [2, 3, 1]
