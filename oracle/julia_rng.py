@@ -24,7 +24,8 @@ reference tree, so each piece is restated here from its published algorithm:
    arrays of up to 383 elements.  Longer arrays are generated straight from the state (see
    `MersenneTwister.raw_array`); that path follows the same runtime but no golden pins it.
 3. `Dict` iteration order: slots in ascending order, a key's home slot is
-   `hash(key) & (sz - 1)` in a table of 16 slots, with linear probing; `hash(::Int64)` is
+   `hash(key) & (sz - 1)` in a table of 16 slots (grown when over 2/3 full), with linear
+   probing; `hash(::Int64)` is
    Thomas Wang's 64-bit integer mix of `3|x| + bits(Float64(x))`.  For monomer ids (1, 2, 3)
    the order is (2, 3, 1); for (1, 2) it is (2, 1).
 

@@ -10,8 +10,9 @@ generation straight from the state, with the last few values taken from the cach
 `randn` is the 256-layer ziggurat of Marsaglia and Tsang (2000) on 52 mantissa bits; its
 tables are in ziggurat_tables.npz (make_ziggurat_tables.py).  For arrays of 13 or more
 elements, `randn!` first draws the whole block, then converts it in order; rejection draws
-follow the block.  `Dict{Int}` iterates its 16 slots in order; a key's slot is its hash (Thomas
-Wang's 64-bit mix of 3|x| + bits(Float64(x))) modulo 16, with linear probing.
+follow the block.  `Dict{Int}` iterates its slots in order (16, growing to max(16, nextpow2(4 count))
+once more than 2/3 are taken); a key's slot is its hash (Thomas Wang's 64-bit mix of
+3|x| + bits(Float64(x))) modulo the table size, with linear probing.
 
 The block generation is vectorised: the dSFMT lung obeys lung' = R(lung) ^ c with R an
 involution (swap the two 64-bit halves and rotate each by 32 bits), so the lungs of a run of
