@@ -22,7 +22,10 @@ def rel(a, b):
 
 PROP = [((64, 1, 1), "lamellar", (10.0,)), ((96, 1, 1), "lamellar", (10.0,)), ((32, 32, 1), "hexagonal", (9.0,)),
         ((64, 32, 1), "rectangular", (12.0, 7.0)), ((16, 16, 16), "cubic", (6.0,)), ((48, 48, 48), "cubic", (8.0,)),
-        ((32, 16, 8), "orthorhombic", (7.0, 5.0, 4.0))]
+        ((32, 16, 8), "orthorhombic", (7.0, 5.0, 4.0)),
+        # odd row counts (a last row without a partner) and partial batches of row pairs
+        ((24, 9, 1), "rectangular", (8.0, 5.0)), ((18, 18, 3), "orthorhombic", (6.0, 6.0, 2.0)),
+        ((36, 27, 9), "orthorhombic", (7.0, 6.0, 3.0))]
 
 
 @pytest.mark.parametrize("dims,crystal,params", PROP, ids=["x".join(map(str, p[0])) for p in PROP])
