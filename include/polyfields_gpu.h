@@ -109,6 +109,12 @@ int pf_set_savepath(pf_system* sys, const char* path);
 /* UnitCell(dim, crystal, params) + add_cell!  (src/system/cell.jl:31-52, system.jl:102-106).
  * crystal is the reference's Symbol name without ':' ("lamellar", "hexagonal", "cubic", ...). */
 int pf_set_cell(pf_system* sys, int dim, const char* crystal, const double* params, int nparams);
+/* ksq!/dksq! (src/system/cell.jl:268-320) fold the y and z frequencies to |j|
+ * (cell.jl:276-277, 306-307), which changes |k|^2 in non-orthogonal cells; the engine does the
+ * same by default (on = 0).  on = 1 uses the signed frequencies j - N above N/2 instead (the
+ * Nyquist index stays +N/2); the bond operators and stress weights are rebuilt on next use.
+ * No counterpart in the reference. */
+int pf_set_signed_k(pf_system* sys, int on);
 /* cell.params, cell.volume (src/system/cell.jl:14-29) */
 int pf_get_cell(const pf_system* sys, double* params, int nparams, double* volume);
 /* R and G basis matrices, row-major 3x3 (src/system/cell.jl:113-118) */

@@ -173,20 +173,25 @@ def ndims_of(dims) -> int:
     return sum(1 for d in dims if d > 1)
 
 
-def folded_indices(dims):
+def folded_indices(dims, signed: bool = False):
     """Folded wavevector indices jx, jy, jz on the half-spectrum grid, each broadcastable to
-    shape (Nz, Ny, Kx).  src/system/cell.jl:273-277 (quirk Q1: |j| instead of signed j)."""
+    shape (Nz, Ny, Kx).  src/system/cell.jl:273-277 (quirk Q1: |j| instead of signed j).  With
+    signed=True the physical signed frequencies (j - N above N/2; the Nyquist index stays +N/2)
+    instead, the option quirk Q1 asks to expose."""
     kx, ny, nz = ksize(dims)
     ix = np.arange(kx, dtype=np.float64)
     iy = np.arange(ny, dtype=np.float64)
     iz = np.arange(nz, dtype=np.float64)
-    jy = np.where(iy <= ny / 2, iy, ny - iy)
-    jz = np.where(iz <= nz / 2, iz, nz - iz)
+    jy = np.where(iy <= ny / 2, iy, iy - ny if signed else ny - iy)
+    jz = np.where(iz <= nz / 2, iz, iz - nz if signed else nz - iz)
     return ix[None, None, :], jy[None, :, None], jz[:, None, None]
 
 
 class UnitCell:
-    """src/system/cell.jl:14-109."""
+    """src/system/cell.jl:14-109.  ``signed_k`` (default False, the reference's fold) switches
+    ksq/dksq to signed frequencies (quirk Q1's option; ``set_signed_k``)."""
+
+    signed_k = False
 
     def __init__(self, dim: int, crystal: str, *params):
         if len(params) == 1 and isinstance(params[0], (list, tuple, np.ndarray)):
@@ -335,9 +340,14 @@ class UnitCell:
                         dGG[i, j, k] += G[l, i] * dG[l, j, k] + G[l, j] * dG[l, i, k]
         self.dRR, self.dGG = dRR, dGG
 
+    def set_signed_k(self, on: bool = True):
+        self.signed_k = bool(on)
+        if self.dims is not None:
+            self.ksq_update()
+
     def ksq_update(self):
-        """ksq! and dksq! (cell.jl:268-320), quirk Q1 fold included."""
-        jx, jy, jz = folded_indices(self.dims)
+        """ksq! and dksq! (cell.jl:268-320), quirk Q1 fold included (unless signed_k)."""
+        jx, jy, jz = folded_indices(self.dims, self.signed_k)
         G = self.G
         # kvec = G * jvec  (G columns are the reciprocal vectors)
         kx = G[0, 0] * jx + G[0, 1] * jy + G[0, 2] * jz

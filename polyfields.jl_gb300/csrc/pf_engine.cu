@@ -415,6 +415,7 @@ struct System {
   Cell cell;
   bool has_cell = false;
   int cell_version = 0;
+  bool signed_k = false;  // ksq/dksq with signed frequencies instead of the reference's fold
   int dksq_version = -1;
 
   std::map<int, std::pair<double, double>> monomers;  // id -> (vol, charge)
@@ -653,6 +654,7 @@ struct System {
     g.ny = ny;
     g.nz = nz;
     g.dim = cell.dim;
+    g.signed_k = signed_k ? 1 : 0;
     for (int i = 0; i < 9; ++i) g.G[i] = cell.G[i];
     for (int i = 0; i < 9 * kMaxParams; ++i) g.dGG[i] = cell.dGG[i];
     return g;
@@ -2442,6 +2444,15 @@ int pf_set_cell(pf_system* sys, int dim, const char* crystal, const double* para
     std::string c(crystal);
     if (!c.empty() && c[0] == ':') c = c.substr(1);
     s.set_cell(dim, c, std::vector<double>(params, params + nparams));
+  });
+}
+
+int pf_set_signed_k(pf_system* sys, int on) {
+  return guard(sys, [&](pf::System& s) {
+    if ((on != 0) != s.signed_k) {
+      s.signed_k = on != 0;
+      ++s.cell_version;  // LD and dksq are rebuilt before their next use
+    }
   });
 }
 

@@ -23,6 +23,7 @@ struct GridDims {
 // reciprocal vector b_c), dGG[(l*3+m)*kMaxParams + p].
 struct CellGeom {
   int nx, ny, nz, dim;
+  int signed_k;  // 0: the reference's folded |j| along y and z (quirk Q1); 1: signed frequencies
   double G[9];
   double dGG[9 * kMaxParams];
 };

@@ -26,7 +26,7 @@ static __global__ void adj_weights_kernel(double* __restrict__ wts, CellGeom g, 
     spectral_index(g, i, ix, iy, iz);
     const double ksq = ksq_at(g, ix, iy, iz);
     const double ld = exp(-ds * b2 * ksq / 6.0) * scale;
-    const double j[3] = {(double)ix, fold_index(iy, g.ny), fold_index(iz, g.nz)};
+    const double j[3] = {(double)ix, fold_index(g, iy, g.ny), fold_index(g, iz, g.nz)};
     for (int p = 0; p < nparams; ++p) {
       double acc = 0.0;
       for (int l = 0; l < g.dim; ++l)

@@ -95,11 +95,15 @@ __global__ void lw_kernel(T* __restrict__ lw, const double* __restrict__ w, doub
     lw[i] = (T)exp(-coeff * w[i]);
 }
 
-// Folded wavevector index of src/system/cell.jl:273-277 (quirk Q1: |j|, not signed j).
-__device__ __forceinline__ double fold_index(int i, int n) { return (double)((i <= n / 2) ? i : n - i); }
+// Wavevector index along y or z: the reference's fold of src/system/cell.jl:273-277 (quirk Q1:
+// |j|, not signed j), or with g.signed_k the signed frequency j - n above n/2 (the Nyquist
+// index stays +n/2).  The two give the same |k|^2 in orthogonal cells.
+__device__ __forceinline__ double fold_index(const CellGeom& g, int i, int n) {
+  return (double)((i <= n / 2) ? i : (g.signed_k ? i - n : n - i));
+}
 
 __device__ __forceinline__ double ksq_at(const CellGeom& g, int ix, int iy, int iz) {
-  const double jx = ix, jy = fold_index(iy, g.ny), jz = fold_index(iz, g.nz);
+  const double jx = ix, jy = fold_index(g, iy, g.ny), jz = fold_index(g, iz, g.nz);
   // kvec = G * jvec, G columns = reciprocal vectors (row-major storage G[r*3+c])
   const double kx = g.G[0] * jx + g.G[1] * jy + g.G[2] * jz;
   const double ky = g.G[3] * jx + g.G[4] * jy + g.G[5] * jz;
@@ -132,7 +136,7 @@ static __global__ void dksq_kernel(double* __restrict__ dk, CellGeom g, int npar
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nk; i += (long)gridDim.x * blockDim.x) {
     int ix, iy, iz;
     spectral_index(g, i, ix, iy, iz);
-    const double j[3] = {(double)ix, fold_index(iy, g.ny), fold_index(iz, g.nz)};
+    const double j[3] = {(double)ix, fold_index(g, iy, g.ny), fold_index(g, iz, g.nz)};
     for (int p = 0; p < nparams; ++p) {
       double acc = 0.0;
       for (int l = 0; l < g.dim; ++l)

@@ -72,6 +72,7 @@ SIGNATURES = {
     "pf_set_savepath": (_c_int, [_vp, ctypes.c_char_p]),
     "pf_set_edwards": (_c_int, [_vp, _c_int, ctypes.c_double]),
     "pf_set_ensemble": (_c_int, [_vp, _c_int]),
+    "pf_set_signed_k": (_c_int, [_vp, _c_int]),
     "pf_euler_create": (_c_int, [_vp, _c_int, ctypes.c_double]),
     "pf_momentum_create": (_c_int, [_vp, _c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double]),

@@ -304,6 +304,12 @@ class FieldSystem:
     def precision(self, value: str) -> None:
         L.check(L.load().pf_set_precision(self._h, _PREC[value]), self._h)
 
+    def set_signed_k(self, on: bool = True) -> None:
+        """Signed y/z frequencies in |k|^2 instead of the reference's |j| fold (cell.jl:276-277,
+        306-307, which changes |k|^2 in non-orthogonal cells); off by default, as in the
+        reference."""
+        L.check(L.load().pf_set_signed_k(self._h, 1 if on else 0), self._h)
+
     def add_cell(self, cell: UnitCell) -> None:
         p = np.ascontiguousarray(cell._params, dtype=np.float64)
         L.check(L.load().pf_set_cell(self._h, cell.dim, cell.crystal.encode(), L.dptr(p), len(p)), self._h)

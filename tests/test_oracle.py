@@ -254,3 +254,47 @@ def test_rqm4_more_accurate_than_rk2():
         return ch.Q
     exact = Q("RQM4", 1600)
     assert abs(Q("RQM4", 50) - exact) < abs(Q("RK2", 50) - exact) / 10
+
+
+# ----------------------------------------------------------------------------- quirk Q1 option
+@pytest.mark.parametrize("dims,crystal,params", [((16, 16, 1), "hexagonal", (9.0,)),
+                                                 ((12, 8, 1), "oblique", (7.0, 5.0, 1.2)),
+                                                 ((8, 6, 6), "triclinic", (5.0, 4.0, 3.0, 1.4, 1.7, 1.3))])
+def test_signed_frequency_option(dims, crystal, params):
+    """Quirk Q1 (cell.jl:276-277, 306-307): the reference folds the y and z frequencies to |j|,
+    which changes |k|^2 in non-orthogonal cells.  The signed option uses j - N above N/2;
+    ksq then equals |G j|^2 over signed integer frequencies, differs from the folded ksq, and
+    dksq stays the parameter derivative of ksq (central differences)."""
+    def cell(p, signed):
+        c = O.UnitCell(sum(1 for d in dims if d > 1), crystal, *p)
+        c.setup(dims)
+        c.set_signed_k(signed)
+        return c
+    c = cell(params, True)
+    kx, ny, nz = O.ksize(dims)
+    jx = np.arange(kx)[None, None, :]
+    jy = np.array([i if i <= ny / 2 else i - ny for i in range(ny)])[None, :, None]
+    jz = np.array([i if i <= nz / 2 else i - nz for i in range(nz)])[:, None, None]
+    k = [c.G[r, 0] * jx + c.G[r, 1] * jy + c.G[r, 2] * jz for r in range(3)]
+    assert np.allclose(c.ksq, k[0] ** 2 + k[1] ** 2 + k[2] ** 2, rtol=1e-13, atol=1e-12)
+    assert not np.allclose(c.ksq, cell(params, False).ksq)
+    h = 1e-6
+    for p in range(len(params)):
+        up, dn = list(params), list(params)
+        up[p] += h
+        dn[p] -= h
+        fd = (cell(up, True).ksq - cell(dn, True).ksq) / (2 * h)
+        assert np.allclose(c.dksq[p], fd, rtol=1e-6, atol=1e-6 * np.max(np.abs(fd))), p
+
+
+def test_signed_frequency_option_changes_nothing_in_orthogonal_cells():
+    for dims, crystal, params in (((32, 1, 1), "lamellar", (10.0,)), ((16, 8, 1), "rectangular", (9.0, 5.0)),
+                                  ((8, 8, 8), "cubic", (6.0,))):
+        a = O.UnitCell(sum(1 for d in dims if d > 1), crystal, *params)
+        a.setup(dims)
+        b = O.UnitCell(sum(1 for d in dims if d > 1), crystal, *params)
+        b.setup(dims)
+        b.set_signed_k(True)
+        assert np.array_equal(a.ksq, b.ksq)
+        for x, y in zip(a.dksq, b.dksq):
+            assert np.array_equal(x, y)
