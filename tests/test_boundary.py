@@ -62,6 +62,8 @@ def test_python_mirror_chain_grid_matches_oracle():
 
 
 def test_python_mirror_rejects_unsorted_dims():
+    """Quirk Q6 (system.jl:55-58): only descending dims work in the reference, which fails on
+    its first size assertion otherwise; the mirror raises the same AssertionError up front."""
     import polyfields as pf
     with pytest.raises(AssertionError):
         pf.FieldSystem((1, 64, 1), pf.UnitCell(1, "lamellar", 10.0))

@@ -123,7 +123,10 @@ def test_cyl2d_seed_gpu():
 
 
 def test_blend3d_density_fp64():
-    """Two species (diblock + homopolymer, Ns=200) on a 3D grid: both chains in one launch."""
+    """Two species (diblock + homopolymer, Ns=200) on a 3D grid: both chains in one launch.
+    The stress carries quirk Q2 (multiblock.jl:279-282: Re*Re products only, and every
+    half-spectrum entry after the k = 0 one doubled, the kx = 0 and Nyquist planes included),
+    as the oracle does."""
     o = SY.blend3d_system(O, n=16)
     g = SY.blend3d_system(pf, n=16, precision="fp64")
     for isp in range(2):
@@ -156,6 +159,8 @@ def test_anderson_steps_fp64(name, kw):
 def test_scft_domain_lamellar_fp64():
     """scft! with Anderson + DomainUpdater on the README lamellar case (README.md:62-79).
 
+    Quirk Q4: DomainUpdater.step! never stops early, so both sides run nper Newton
+    iterations per update (domain.jl:59-89).
     The DomainUpdater's finite-difference Jacobian (dx = 1e-8, domain.jl:101) multiplies the
     rounding error of the stress by 1e8, so two correct FP64 implementations that sum in a
     different order follow cell trajectories that agree to ~1e-7 relative, not to 1e-10."""

@@ -88,8 +88,9 @@ def test_oracle_reproduces_test_updaters_goldens():
 
 def test_oracle_replays_the_notebooks_seeded_momentum_run():
     """examples/examples.ipynb cells 11-12 from the seed: every line scft! printed (the state
-    after k updates, formatted as the reference formats it), the convergence step and the
-    returned SCFTResults.  About 20 s: 3273 MomentumUpdater steps of the 256-point blend."""
+    after k updates, formatted as the reference formats it; quirk Q5: inside the loop ferr and
+    fhelm come from the residuals of the pre-update field, simulate.jl:92-107), the convergence
+    step and the returned SCFTResults.  About 20 s: 3273 MomentumUpdater steps of the 256-point blend."""
     run = RV.NOTEBOOK_BLEND_RUN
     sys = W.notebook_blend_seeded_system(O)
     sys.residuals_update()  # scft! starts with residuals!(sys) (simulate.jl:66)
